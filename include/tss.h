@@ -1,0 +1,205 @@
+/*
+ * tss.h -- C ABI of the GB300-native two-scale WCSPH solver.
+ *
+ * The surface mirrors the reference's WCSPHConfig / ParticleSystem / WCSPHSolver
+ * classes (TwoScale2D/WCSPHSolver.h:14-131, TwoScale2D/ParticleSystem.h:17-86):
+ * build a configuration, construct a solver from particle arrays, advance steps,
+ * and read device buffers for an (optional) renderer.  Every entry point returns a
+ * tss_status; no C++ exception crosses this boundary.  Host arrays passed in are
+ * copied; the solver owns all device memory it allocates.
+ *
+ * Threading: one solver handle per host thread; handles share no state.
+ */
+#ifndef TSS_H
+#define TSS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference threw std::runtime_error (stdutil.h:22-33,
+ * CUDA/cuda.h:37-51) and printed + paused in CheckLastError (cuda.h:24-35). */
+typedef enum tss_status {
+    TSS_OK = 0,
+    TSS_INVALID_ARG = 1,   /* bad argument or configuration                      */
+    TSS_OOM = 2,           /* device or host allocation failed                    */
+    TSS_CUDA_ERROR = 3,    /* a CUDA runtime call failed                          */
+    TSS_CAPACITY = 4,      /* a particle pool would overflow its capacity         */
+    TSS_NUMERIC = 5,       /* NaN/Inf in a density, pressure or acceleration      */
+    TSS_TIMEOUT = 6,       /* a bounded device-side wait gave up                  */
+    TSS_NO_DEVICE = 7      /* no CUDA device                                      */
+} tss_status;
+
+/* Configuration flags. */
+#define TSS_FLAG_Q1_COMPAT 0x1u
+/* TSS_FLAG_Q1_COMPAT: compute the high-res density's low-res term the way the
+ * reference does (TwoScale2D/WCSPHSolver.cu:1483-1510): it iterates the HIGH-res
+ * sorted list over LOW-grid cell ranges (including the never-written identity
+ * tail of that list) and accumulates into the high-res sum, while the low-res
+ * term stays zero.  Without the flag the term uses the low-res particles, as the
+ * kernel's parameter list intends. */
+
+/* Solver parameters.  Mirrors WCSPHConfig (TwoScale2D/WCSPHSolver.h:14-35) plus the
+ * constants the reference hard-codes (gravity 9.81: WCSPHSolver.cu:1805,2012; split
+ * half-plane x > 0.5: WCSPHSolver.cu:1835; relax 4 x dt/10:
+ * TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:2380-2446). */
+typedef struct tss_config {
+    float domain_origin[2];
+    float domain_end[2];
+    int   dims_low[2];        /* ceil((end - origin) / r_low)   (WCSPHSolver.cu:2323-2326) */
+    int   dims_high[2];       /* ceil((end - origin) / r_high)  (WCSPHSolver.cu:2328-2331) */
+    float r_low;              /* EffectiveRadius: support radius of the low-res scale      */
+    float r_high;             /* EffectiveRadiusHigh                                        */
+    float rest_density;
+    float tait_b;             /* Tait coefficient B in p = B((rho/rho0)^7 - 1)              */
+    float speed_sound;
+    float alpha;              /* artificial viscosity                                       */
+    float tension;            /* "tension" coefficient sigma                                */
+    float dt;
+    float gravity;            /* subtracted from a_y; the reference hard-codes 9.81f        */
+    float roi[4];             /* split region x0,y0,x1,y1: open rectangle on the predicted  */
+                              /* position; {0.5,-inf,inf,inf} is the reference's x > 0.5    */
+    int   relax_iters;        /* relaxation sub-steps for newly created high-res particles  */
+                              /* (0 = the current reference tree, 4 = its older snapshot)   */
+    float relax_dt_div;       /* relaxation sub-step = dt / relax_dt_div (10 in reference)  */
+    unsigned flags;           /* TSS_FLAG_*                                                 */
+} tss_config;
+
+/* Fill *cfg like WCSPHConfig::WCSPHConfig (TwoScale2D/WCSPHSolver.cu:2287-2332):
+ * rejects xs >= xe or ys >= ye, derives both grids' dimensions by ceil, and sets
+ * the reference's hard-coded constants (gravity 9.81, ROI x > 0.5, no relaxation,
+ * relax_dt_div 10, TSS_FLAG_Q1_COMPAT). */
+tss_status tss_config_init(tss_config* cfg, float xs, float ys, float xe, float ye,
+                           float effective_radius, float effective_radius_high,
+                           float rest_density, float tait_coeff, float speed_sound,
+                           float alpha, float tension_coefficient, float time_step);
+
+/* ------------------------------------------------------------------------- */
+/* Solver                                                                     */
+/* ------------------------------------------------------------------------- */
+typedef struct tss_solver tss_solver;
+
+/* Construct a solver.  Replaces `new ParticleSystem` x3 + CreateParticleBox(Canvas) +
+ * WCSPHSolver ctor + Bind() (ParticleSystem.cpp:13-179, WCSPHSolver.cu:2391-2639).
+ *   low_pos, low_vel : host, 2*n_low floats (x,y interleaved); low_vel may be NULL (= 0)
+ *   cap_high         : high-res pool capacity (the reference uses 4 * n_low)
+ *   wall_pos         : host, 2*n_wall floats, the fixed boundary particles
+ * Low-res particle i gets slot id i; its children get high-res slot ids 4*i+0..3. */
+tss_status tss_solver_create(const tss_config* cfg,
+                             int n_low, const float* low_pos, const float* low_vel,
+                             float mass_low, int cap_high, float mass_high,
+                             int n_wall, const float* wall_pos, float mass_wall,
+                             tss_solver** out);
+void tss_solver_destroy(tss_solver* s);
+
+/* Advance n_steps steps (WCSPHSolver::AdvanceTS, WCSPHSolver.cu:2726-2810), enqueued
+ * on `stream` (a cudaStream_t; NULL = the solver's own stream).  Nothing is copied
+ * back to the host; the particle counts stay on the device.  The first call
+ * captures the step into a CUDA graph; later calls replay it. */
+tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream);
+
+/* Block until all enqueued work is done; returns the device error word mapped to a
+ * status (TSS_CAPACITY, TSS_NUMERIC, TSS_TIMEOUT) or TSS_OK. */
+tss_status tss_solver_sync(tss_solver* s);
+
+typedef struct tss_counts {
+    int n_low;                /* low-res particles (constant)                         */
+    int n_high;               /* high-res particles                                   */
+    int n_transient_low;      /* low-res particles in state 1 (split parents)         */
+    int n_split_last;         /* parents split in the last step                       */
+    long long steps;          /* steps taken                                          */
+    unsigned error_bits;      /* device error word (TSS_ERR_*)                        */
+} tss_counts;
+
+#define TSS_ERR_CAPACITY 0x1u /* a split would overflow the high-res pool            */
+#define TSS_ERR_NUMERIC  0x2u /* NaN/Inf density, pressure or acceleration            */
+#define TSS_ERR_TIMEOUT  0x4u /* a bounded device-side wait gave up                   */
+
+tss_status tss_solver_counts(tss_solver* s, tss_counts* out);
+
+/* Particle state of one scale, in list order (the order the next step starts from:
+ * this step's sorted order, with newly created children appended to the high list).
+ * Caller-owned host buffers with room for n entries (pos/vel: 2n floats). */
+typedef struct tss_scale_state {
+    int       n;
+    int32_t*  id;             /* slot ids                                              */
+    float*    pos;            /* 2n                                                    */
+    float*    vel;            /* 2n                                                    */
+    uint8_t*  state;          /* 0 default, 1 transient, 2 deleted                     */
+    float*    dens;           /* last densities (may be NULL)                          */
+    float*    pres;           /* last pressures (may be NULL)                          */
+} tss_scale_state;
+
+#define TSS_SCALE_LOW  0
+#define TSS_SCALE_HIGH 1
+
+/* Download / replace the state of one scale (checkpoint and per-step resync).
+ * Upload checks ids are unique and in range and sets the count. */
+tss_status tss_solver_download(tss_solver* s, int scale, tss_scale_state* out);
+tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in);
+
+/* The low-res parents split in the last step; their children are relaxed at the
+ * start of the next step when relax_iters > 0. */
+tss_status tss_solver_get_fresh(tss_solver* s, int* n, int32_t* parents /* may be NULL */);
+tss_status tss_solver_set_fresh(tss_solver* s, int n, const int32_t* parents);
+
+/* Per-step intermediate buffers, for parity checks (host copies). */
+typedef enum tss_buffer {
+    TSS_BUF_SORTED_ID = 0,    /* int32[n]   ids in (cell, id) order, the sorted list    */
+    TSS_BUF_CELL_OFFSET = 1,  /* int32[C+1] dense cell offsets (start = off[c],         */
+                              /*            end = off[c+1])                             */
+    TSS_BUF_DENSITY = 2,      /* float[n]   densities, sorted order                     */
+    TSS_BUF_PRESSURE = 3,     /* float[n]   pressures, sorted order                     */
+    TSS_BUF_ACCEL = 4,        /* float[2n]  accelerations, sorted order                 */
+    TSS_BUF_SPLIT = 5,        /* int32[k]   low-res slot ids split this step (low only) */
+    TSS_BUF_WALL_CELL_OFFSET = 6 /* int32[C_low+1] boundary cell offsets (low only)     */
+} tss_buffer;
+/* Copies buffer `which` of `scale` into `dst` (capacity `count` elements); *written
+ * receives the element count (may be NULL).  Values refer to the last step. */
+tss_status tss_solver_copy(tss_solver* s, int scale, int which, void* dst, size_t count,
+                           size_t* written);
+
+/* Device pointers for a renderer (replaces the GL VBO interop of
+ * ParticleSystem.cpp:20-46,78-98).  Valid until the next tss_solver_step. */
+typedef struct tss_buffers {
+    const float*   pos[2];    /* float2[n], list order                                 */
+    const float*   vel[2];
+    const float*   dens[2];   /* float[n], sorted order of the last step               */
+    const int32_t* id[2];     /* int32[n], list order                                  */
+    const uint8_t* state[2];
+    const int*     counts;    /* device int[2] = {n_low, n_high}                       */
+} tss_buffers;
+tss_status tss_solver_device_buffers(tss_solver* s, tss_buffers* out);
+
+/* Last error message of this handle (NUL-terminated, truncated to len). */
+tss_status tss_solver_last_error(tss_solver* s, char* buf, int len);
+const char* tss_status_string(tss_status st);
+
+/* ------------------------------------------------------------------------- */
+/* Grid build on caller-owned device memory                                   */
+/* ------------------------------------------------------------------------- */
+/* Uniform-grid neighbour structure of n particles, replacing computeParticleHash +
+ * thrust::sort_by_key + computeCellStartEndIndices (WCSPHSolver.cu:1246-1340,
+ * 2814-2854).  cell(p) = clamp(int((p - origin)/cell_size), 0, dim-1) per axis,
+ * hash = cy*dimx + cx (WCSPHSolver.cu:241-296).  Outputs, all device memory:
+ *   d_order[n]       : source index of each sorted position; the order is by
+ *                      (cell, d_id) ascending, i.e. a stable sort by cell of an
+ *                      id-ascending list
+ *   d_cell_off[C+1]  : dense offsets: particles of cell c are order[off[c]..off[c+1])
+ *                      (the reference's cellStart/cellEnd, with empty cells as
+ *                      empty ranges instead of -1)
+ * d_id holds distinct ids (any non-negative int32); d_workspace is scratch of
+ * tss_grid_workspace_size bytes.  Enqueued on `stream`; nothing is synchronised. */
+tss_status tss_grid_workspace_size(int n, int dimx, int dimy, size_t* bytes);
+tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, int n,
+                          float origin_x, float origin_y, float cell_size,
+                          int dimx, int dimy, int32_t* d_order, int32_t* d_cell_off,
+                          void* d_workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TSS_H */

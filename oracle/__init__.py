@@ -1,0 +1,220 @@
+"""ORACLE -- test infrastructure only.
+
+Python handles for
+  * Oracle: the CPU restatement of the two-scale WCSPH step (tss_oracle.cpp),
+    FP32 (the reference's arithmetic, bit for bit) or FP64 (error reference);
+  * RefCPU: the reference's own kernel source compiled for the CPU and driven by
+    a headless harness (refcpu/), available only where the reference checkout is.
+
+Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package; the product (twoscalesplit_gb300) never does.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_ORC = None
+_REF = None
+
+
+def _orc_lib():
+    global _ORC
+    if _ORC is None:
+        path = _build.build_oracle()
+        lib = ctypes.CDLL(path)
+        vp, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        lib.orc_create.restype = vp
+        lib.orc_create.argtypes = [vp, i, f, f, i, i, i, vp, f]
+        lib.orc_destroy.argtypes = [vp]
+        lib.orc_set_scale.argtypes = [vp, i, i, vp, vp, vp, vp, vp, vp]
+        lib.orc_set_fresh.argtypes = [vp, i, vp]
+        lib.orc_step.argtypes = [vp]
+        lib.orc_get.argtypes = [vp, i, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        lib.orc_set_threads.argtypes = [i]
+        lib.orc_max_threads.restype = i
+        lib.orc_grid.argtypes = [i, vp, vp, f, f, f, i, i, vp, vp]
+        _ORC = lib
+    return _ORC
+
+
+def _ref_lib():
+    global _REF
+    if _REF is None:
+        path = _build.build_refcpu()
+        if path is None:
+            return None
+        lib = ctypes.CDLL(path)
+        vp, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        lib.ref_create.restype = vp
+        lib.ref_create.argtypes = [vp, i, f, i, f, i, vp, f]
+        lib.ref_destroy.argtypes = [vp]
+        lib.ref_set_scale.argtypes = [vp, i, i, vp, vp, vp, vp, vp, vp]
+        lib.ref_set_fresh.argtypes = [vp, i, vp]
+        lib.ref_step.argtypes = [vp]
+        lib.ref_get.argtypes = [vp, i, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        lib.ref_grid.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
+        _REF = lib
+    return _REF
+
+
+def refcpu_available():
+    return _ref_lib() is not None
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def set_threads(n):
+    _orc_lib().orc_set_threads(int(n))
+
+
+def max_threads():
+    return _orc_lib().orc_max_threads()
+
+
+def grid(pos, ids, origin, cell, dims):
+    """(cell, id) order and dense cell offsets, FP32 (orc_grid)."""
+    lib = _orc_lib()
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    n = ids.shape[0]
+    order = np.empty(n, np.int32)
+    off = np.empty(dims[0] * dims[1] + 1, np.int32)
+    lib.orc_grid(n, _p(pos), _p(ids), origin[0], origin[1], cell, dims[0], dims[1], _p(order), _p(off))
+    return order, off
+
+
+class Oracle:
+    """One scene in the CPU oracle.  State arrays are in list order."""
+
+    def __init__(self, scene, precision=32):
+        self.lib = _orc_lib()
+        self.scene = scene
+        self.precision = precision
+        walls = np.ascontiguousarray(scene.wall_pos, dtype=np.float32)
+        self._cfg = scene.config
+        self.h = self.lib.orc_create(ctypes.byref(scene.config), precision, scene.mass_low, scene.mass_high,
+                                     scene.n_low, scene.cap_high, walls.shape[0], _p(walls), scene.mass_wall)
+        n = scene.n_low
+        self.set_scale(0, np.arange(n, dtype=np.int32), scene.low_pos, scene.low_vel, np.zeros(n, np.uint8))
+        self.set_scale(1, np.zeros(0, np.int32), np.zeros((0, 2)), np.zeros((0, 2)), np.zeros(0, np.uint8))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def set_scale(self, scale, ids, pos, vel, state, dens=None, pres=None):
+        ids = np.ascontiguousarray(ids, np.int32)
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1)
+        vel = np.ascontiguousarray(vel, np.float64).reshape(-1)
+        state = np.ascontiguousarray(state, np.uint8)
+        dens = None if dens is None else np.ascontiguousarray(dens, np.float64)
+        pres = None if pres is None else np.ascontiguousarray(pres, np.float64)
+        st = self.lib.orc_set_scale(self.h, scale, ids.shape[0], _p(ids), _p(pos), _p(vel), _p(state),
+                                    _p(dens), _p(pres))
+        if st != 0:
+            raise ValueError(f"orc_set_scale failed ({st})")
+
+    def set_fresh(self, parents):
+        parents = np.ascontiguousarray(parents, np.int32)
+        self.lib.orc_set_fresh(self.h, parents.shape[0], _p(parents))
+
+    def step(self):
+        return self.lib.orc_step(self.h)
+
+    _INT = {"id", "sorted_src", "sorted_id", "cell_off", "split", "fresh", "wall_cell_off"}
+    _U8 = {"state"}
+
+    def get(self, scale, name):
+        n = ctypes.c_size_t(0)
+        self.lib.orc_get(self.h, scale, name.encode(), None, 0, ctypes.byref(n))
+        if name in self._INT:
+            out = np.empty(n.value, np.int32)
+        elif name in self._U8:
+            out = np.empty(n.value, np.uint8)
+        else:
+            out = np.empty(n.value, np.float64)
+        self.lib.orc_get(self.h, scale, name.encode(), _p(out), n.value, ctypes.byref(n))
+        if name in ("pos", "vel", "acc"):
+            out = out.reshape(-1, 2)
+        return out
+
+    def state(self, scale):
+        return {k: self.get(scale, k) for k in ("id", "pos", "vel", "state", "dens_state", "pres_state")}
+
+    def load_state(self, scale, st):
+        self.set_scale(scale, st["id"], st["pos"], st["vel"], st["state"], st.get("dens_state"),
+                       st.get("pres_state"))
+
+
+def ref_grid(config, pos_by_slot, ids):
+    """The reference's own grid build (hash, stable sort, cell start/end), CPU."""
+    lib = _ref_lib()
+    pos = np.ascontiguousarray(pos_by_slot, np.float32)
+    ids = np.ascontiguousarray(ids, np.int32)
+    n = ids.shape[0]
+    cells = config.dims_low[0] * config.dims_low[1]
+    sid = np.empty(n, np.int32)
+    sh = np.empty(n, np.int32)
+    cs = np.empty(cells, np.int32)
+    ce = np.empty(cells, np.int32)
+    lib.ref_grid(ctypes.byref(config), n, _p(pos), _p(ids), _p(sid), _p(sh), _p(cs), _p(ce))
+    return sid, sh, cs, ce
+
+
+class RefCPU:
+    """The reference's kernels run on the CPU (slot-indexed arrays, as the reference)."""
+
+    def __init__(self, scene):
+        self.lib = _ref_lib()
+        if self.lib is None:
+            raise RuntimeError("reference checkout not available")
+        walls = np.ascontiguousarray(scene.wall_pos, dtype=np.float32)
+        self.scene = scene
+        self.h = self.lib.ref_create(ctypes.byref(scene.config), scene.n_low, scene.mass_low, 4 * scene.n_low,
+                                     scene.mass_high, walls.shape[0], _p(walls), scene.mass_wall)
+        n = scene.n_low
+        self.set_scale(0, np.arange(n, dtype=np.int32), scene.low_pos, scene.low_vel, np.zeros(n, np.uint8))
+        self.set_scale(1, np.zeros(0, np.int32), np.zeros((0, 2)), np.zeros((0, 2)), np.zeros(0, np.uint8))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.ref_destroy(self.h)
+            self.h = None
+
+    def set_scale(self, scale, ids, pos, vel, state, dens=None, pres=None):
+        ids = np.ascontiguousarray(ids, np.int32)
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1)
+        vel = np.ascontiguousarray(vel, np.float32).reshape(-1)
+        state = np.ascontiguousarray(state, np.uint8)
+        dens = None if dens is None else np.ascontiguousarray(dens, np.float32)
+        pres = None if pres is None else np.ascontiguousarray(pres, np.float32)
+        st = self.lib.ref_set_scale(self.h, scale, ids.shape[0], _p(ids), _p(pos), _p(vel), _p(state),
+                                    _p(dens), _p(pres))
+        if st != 0:
+            raise ValueError("ref_set_scale failed")
+
+    def set_fresh(self, parents):
+        parents = np.ascontiguousarray(parents, np.int32)
+        self.lib.ref_set_fresh(self.h, parents.shape[0], _p(parents))
+
+    def step(self):
+        self.lib.ref_step(self.h)
+
+    _U8 = {"state"}
+    _F = {"pos", "vel", "acc", "dens", "pres"}
+
+    def get(self, scale, name):
+        n = ctypes.c_size_t(0)
+        self.lib.ref_get(self.h, scale, name.encode(), None, 0, ctypes.byref(n))
+        dt = np.uint8 if name in self._U8 else (np.float32 if name in self._F else np.int32)
+        out = np.empty(n.value, dt)
+        self.lib.ref_get(self.h, scale, name.encode(), _p(out), n.value, ctypes.byref(n))
+        if name in ("pos", "vel", "acc"):
+            out = out.reshape(-1, 2)
+        return out

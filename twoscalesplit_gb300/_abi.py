@@ -1,0 +1,193 @@
+"""ctypes view of the C ABI declared in include/tss.h, and the library loader.
+
+The shared library (libtss.so, built in-tree by twoscalesplit_gb300.build) holds
+the sm_103a kernels and the host solver.  There is no CPU fallback: every call
+that needs the library raises TssError when it cannot be loaded.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libtss.so")
+
+TSS_OK = 0
+TSS_INVALID_ARG = 1
+TSS_OOM = 2
+TSS_CUDA_ERROR = 3
+TSS_CAPACITY = 4
+TSS_NUMERIC = 5
+TSS_TIMEOUT = 6
+TSS_NO_DEVICE = 7
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "CAPACITY",
+                5: "NUMERIC", 6: "TIMEOUT", 7: "NO_DEVICE"}
+
+TSS_FLAG_Q1_COMPAT = 0x1
+TSS_SCALE_LOW = 0
+TSS_SCALE_HIGH = 1
+
+TSS_BUF_SORTED_ID = 0
+TSS_BUF_CELL_OFFSET = 1
+TSS_BUF_DENSITY = 2
+TSS_BUF_PRESSURE = 3
+TSS_BUF_ACCEL = 4
+TSS_BUF_SPLIT = 5
+TSS_BUF_WALL_CELL_OFFSET = 6
+
+TSS_ERR_CAPACITY = 0x1
+TSS_ERR_NUMERIC = 0x2
+TSS_ERR_TIMEOUT = 0x4
+
+
+class TssError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__(f"tss status {STATUS_NAMES.get(status, status)}{': ' + msg if msg else ''}")
+
+
+class TssConfig(ctypes.Structure):
+    """struct tss_config (include/tss.h)."""
+    _fields_ = [
+        ("domain_origin", ctypes.c_float * 2),
+        ("domain_end", ctypes.c_float * 2),
+        ("dims_low", ctypes.c_int * 2),
+        ("dims_high", ctypes.c_int * 2),
+        ("r_low", ctypes.c_float),
+        ("r_high", ctypes.c_float),
+        ("rest_density", ctypes.c_float),
+        ("tait_b", ctypes.c_float),
+        ("speed_sound", ctypes.c_float),
+        ("alpha", ctypes.c_float),
+        ("tension", ctypes.c_float),
+        ("dt", ctypes.c_float),
+        ("gravity", ctypes.c_float),
+        ("roi", ctypes.c_float * 4),
+        ("relax_iters", ctypes.c_int),
+        ("relax_dt_div", ctypes.c_float),
+        ("flags", ctypes.c_uint),
+    ]
+
+    def as_dict(self):
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+class TssCounts(ctypes.Structure):
+    _fields_ = [("n_low", ctypes.c_int), ("n_high", ctypes.c_int), ("n_transient_low", ctypes.c_int),
+                ("n_split_last", ctypes.c_int), ("steps", ctypes.c_longlong), ("error_bits", ctypes.c_uint)]
+
+
+class TssScaleState(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("id", ctypes.POINTER(ctypes.c_int32)),
+                ("pos", ctypes.POINTER(ctypes.c_float)), ("vel", ctypes.POINTER(ctypes.c_float)),
+                ("state", ctypes.POINTER(ctypes.c_uint8)), ("dens", ctypes.POINTER(ctypes.c_float)),
+                ("pres", ctypes.POINTER(ctypes.c_float))]
+
+
+class TssBuffers(ctypes.Structure):
+    _fields_ = [("pos", ctypes.c_void_p * 2), ("vel", ctypes.c_void_p * 2), ("dens", ctypes.c_void_p * 2),
+                ("id", ctypes.c_void_p * 2), ("state", ctypes.c_void_p * 2), ("counts", ctypes.c_void_p)]
+
+
+def config_init(xs, ys, xe, ye, effective_radius, effective_radius_high, rest_density, tait_coeff,
+                speed_sound, alpha, tension_coefficient, time_step):
+    """Python restatement of tss_config_init (same float32 arithmetic), so host code
+    that only needs a configuration does not have to load the CUDA library.
+    Mirrors WCSPHConfig::WCSPHConfig (TwoScale2D/WCSPHSolver.cu:2287-2332)."""
+    f = np.float32
+    if not (f(xs) < f(xe) and f(ys) < f(ye)):
+        raise ValueError("Invalid configuration parameters")
+    if not (f(effective_radius) > 0 and f(effective_radius_high) > 0):
+        raise ValueError("Invalid configuration parameters")
+    c = TssConfig()
+    c.domain_origin[:] = [xs, ys]
+    c.domain_end[:] = [xe, ye]
+    for name, r in (("dims_low", effective_radius), ("dims_high", effective_radius_high)):
+        dx = np.float32(np.float32(xe) - np.float32(xs)) / np.float32(r)
+        dy = np.float32(np.float32(ye) - np.float32(ys)) / np.float32(r)
+        getattr(c, name)[:] = [int(math.ceil(np.float32(dx))), int(math.ceil(np.float32(dy)))]
+    c.r_low = effective_radius
+    c.r_high = effective_radius_high
+    c.rest_density = rest_density
+    c.tait_b = tait_coeff
+    c.speed_sound = speed_sound
+    c.alpha = alpha
+    c.tension = tension_coefficient
+    c.dt = time_step
+    c.gravity = 9.81
+    c.roi[:] = [0.5, -math.inf, math.inf, math.inf]
+    c.relax_iters = 0
+    c.relax_dt_div = 10.0
+    c.flags = TSS_FLAG_Q1_COMPAT
+    return c
+
+
+_LIB = None
+
+
+def load_library(path=None):
+    """Load libtss.so; raises TssError(TSS_NO_DEVICE...) style errors loudly if absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise TssError(TSS_CUDA_ERROR, f"{p} not built (run twoscalesplit_gb300.build.build())")
+    lib = ctypes.CDLL(p)
+    vp, i, f, u = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_uint
+    fp = ctypes.POINTER(ctypes.c_float)
+    ip = ctypes.POINTER(ctypes.c_int32)
+    cfgp = ctypes.POINTER(TssConfig)
+    sig = {
+        "tss_config_init": (i, [cfgp, f, f, f, f, f, f, f, f, f, f, f, f]),
+        "tss_solver_create": (i, [cfgp, i, fp, fp, f, i, f, i, fp, f, ctypes.POINTER(vp)]),
+        "tss_solver_destroy": (None, [vp]),
+        "tss_solver_step": (i, [vp, i, vp]),
+        "tss_solver_sync": (i, [vp]),
+        "tss_solver_counts": (i, [vp, ctypes.POINTER(TssCounts)]),
+        "tss_solver_download": (i, [vp, i, ctypes.POINTER(TssScaleState)]),
+        "tss_solver_upload": (i, [vp, i, ctypes.POINTER(TssScaleState)]),
+        "tss_solver_get_fresh": (i, [vp, ctypes.POINTER(i), ip]),
+        "tss_solver_set_fresh": (i, [vp, i, ip]),
+        "tss_solver_copy": (i, [vp, i, i, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "tss_solver_device_buffers": (i, [vp, ctypes.POINTER(TssBuffers)]),
+        "tss_solver_last_error": (i, [vp, ctypes.c_char_p, i]),
+        "tss_status_string": (ctypes.c_char_p, [i]),
+        "tss_grid_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
+        "tss_grid_build": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp, ctypes.c_size_t, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    del u
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def check(status, solver=None, lib=None):
+    if status != TSS_OK:
+        msg = ""
+        if solver is not None and lib is not None:
+            buf = ctypes.create_string_buffer(512)
+            lib.tss_solver_last_error(solver, buf, 512)
+            msg = buf.value.decode(errors="replace")
+        raise TssError(status, msg)
+
+
+def fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if a is not None else None
+
+
+def u8ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) if a is not None else None

@@ -1,0 +1,136 @@
+"""Seeded scene generators: the dam-break workloads the solver is measured on.
+
+The lattice and wall generators restate the reference's CreateParticleBox and
+CreateParticleBoxCanvas (TwoScale2D/ParticleSystem.cpp:123-179); the dam-break
+parameters follow the reference's scene setup (TwoScale2D/main.cpp:144-175) with
+the constants of the named workloads:
+
+  dam_break_5k    50x100 lattice (5,000 low-res particles), spacing 0.008,
+                  [0,0.4]x[0,0.8] in the unit box, ROI [0.4,0.7]x[0,0.3], dt 1e-4,
+                  2,000 steps, children relaxed 4 x dt/10 before coupling
+  dam_break_1m    707x1414 lattice (999,698 particles), spacing 5.66e-4,
+                  ROI [0.4,0.9]x[0,0.5], high-res pool 4M, 500 steps
+
+Common constants: rest density 1000, Tait gamma 7, c = 10*sqrt(2*9.81*0.8),
+B = rho0*c^2/7, alpha 0.05, sigma 0.08 (main.cpp:153), gravity 9.81, support
+2 x spacing, high-res support and spacing halved, mass/4 per child.  Walls are 3
+layers of fixed particles around [0,1]^2 at half the fluid spacing; the grid
+domain is padded by 4 wall spacings so that the walls lie inside it.  Every
+lattice coordinate is jittered by U(+-1e-4 * spacing) from the seed.
+dt for dam_break_1m keeps the Courant number of dam_break_5k: dt = 1e-4 * dx/0.008.
+"""
+import dataclasses
+import math
+
+import numpy as np
+
+from ._abi import TssConfig, config_init
+
+REST_DENSITY = 1000.0
+GAMMA = 7
+SPEED_SOUND = 10.0 * math.sqrt(2.0 * 9.81 * 0.8)
+TAIT_B = REST_DENSITY * SPEED_SOUND ** 2 / GAMMA
+ALPHA = 0.05
+SIGMA = 0.08
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    config: TssConfig
+    low_pos: np.ndarray        # float32 [n, 2]
+    low_vel: np.ndarray        # float32 [n, 2]
+    mass_low: float
+    mass_high: float
+    cap_high: int
+    wall_pos: np.ndarray       # float32 [nw, 2]
+    mass_wall: float
+    steps: int
+    dx: float
+
+    @property
+    def n_low(self):
+        return int(self.low_pos.shape[0])
+
+    @property
+    def n_wall(self):
+        return int(self.wall_pos.shape[0])
+
+
+def particle_box(xs, ys, dx, dim_x, dim_y):
+    """CreateParticleBox (ParticleSystem.cpp:123-148): row-major lattice, j outer."""
+    f = np.float32
+    i = np.arange(dim_x, dtype=np.float32)
+    j = np.arange(dim_y, dtype=np.float32)
+    gx = f(xs) + f(dx) * i[None, :]
+    gy = f(ys) + f(dx) * j[:, None]
+    pos = np.empty((dim_y, dim_x, 2), dtype=np.float32)
+    pos[..., 0] = np.broadcast_to(gx, (dim_y, dim_x))
+    pos[..., 1] = np.broadcast_to(gy, (dim_y, dim_x))
+    return pos.reshape(-1, 2)
+
+
+def particle_box_canvas(xs, ys, dx, dim_x, dim_y, off_x, off_y):
+    """CreateParticleBoxCanvas (ParticleSystem.cpp:150-179): the ring of lattice
+    points around a dim_x x dim_y interior, off_x/off_y layers thick."""
+    f = np.float32
+    out = []
+    for j in range(-off_y, dim_y + off_y):
+        i = np.arange(-off_x, dim_x + off_x)
+        if 0 <= j < dim_y:
+            i = i[(i < 0) | (i >= dim_x)]
+        p = np.empty((i.size, 2), dtype=np.float32)
+        p[:, 0] = f(xs) + f(dx) * i.astype(np.float32)
+        p[:, 1] = f(ys) + f(dx) * f(j)
+        out.append(p)
+    return np.concatenate(out, axis=0)
+
+
+def _dam_break(name, nx, ny, dx, roi, dt, steps, cap_high, relax_iters, seed, flags=None):
+    rng = np.random.default_rng(seed)
+    dx = float(np.float32(dx))
+    low = particle_box(0.5 * dx, 0.5 * dx, dx, nx, ny)
+    low = low + rng.uniform(-1e-4 * dx, 1e-4 * dx, size=low.shape).astype(np.float32)
+    low = low.astype(np.float32)
+    wdx = 0.5 * dx
+    nw = int(math.ceil(1.0 / wdx)) + 1
+    walls = particle_box_canvas(0.0, 0.0, wdx, nw, nw, 3, 3)
+    pad = 4 * wdx
+    r = 2.0 * dx
+    cfg = config_init(-pad, -pad, (nw - 1) * wdx + pad, (nw - 1) * wdx + pad, r, 0.5 * r,
+                      REST_DENSITY, TAIT_B, SPEED_SOUND, ALPHA, SIGMA, dt)
+    cfg.roi[:] = roi
+    cfg.relax_iters = relax_iters
+    if flags is not None:
+        cfg.flags = flags
+    m = REST_DENSITY * dx * dx
+    return Scene(name=name, config=cfg, low_pos=low, low_vel=np.zeros_like(low), mass_low=m,
+                 mass_high=m / 4.0, cap_high=cap_high, wall_pos=walls,
+                 mass_wall=REST_DENSITY * wdx * wdx, steps=steps, dx=dx)
+
+
+def dam_break_5k(seed=0, **kw):
+    return _dam_break("dam_break_5k", 50, 100, 0.008, [0.4, 0.0, 0.7, 0.3], 1e-4, 2000,
+                      4 * 5000, 4, seed, **kw)
+
+
+def dam_break_1m(seed=0, **kw):
+    dx = 5.66e-4
+    return _dam_break("dam_break_1m", 707, 1414, dx, [0.4, 0.0, 0.9, 0.5], 1e-4 * dx / 0.008, 500,
+                      4_000_000, 4, seed, **kw)
+
+
+def dam_break_small(nx, ny, dx=None, seed=0, roi=None, relax_iters=4, cap_high=None, **kw):
+    """A dam break of any lattice size filling [0,0.4]x[0,0.8] (test cases)."""
+    if dx is None:
+        dx = 0.4 / nx
+    roi = roi if roi is not None else [0.4, 0.0, 0.7, 0.3]
+    return _dam_break(f"dam_break_{nx}x{ny}", nx, ny, dx, roi, 1e-4 * dx / 0.008, 100,
+                      cap_high if cap_high is not None else 4 * nx * ny, relax_iters, seed, **kw)
+
+
+SCENES = {"dam_break_5k": dam_break_5k, "dam_break_1m": dam_break_1m}
+
+
+def make_scene(name, seed=0, **kw):
+    return SCENES[name](seed=seed, **kw)

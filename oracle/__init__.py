@@ -36,6 +36,8 @@ def _orc_lib():
         lib.orc_set_threads.argtypes = [i]
         lib.orc_max_threads.restype = i
         lib.orc_grid.argtypes = [i, vp, vp, f, f, f, i, i, vp, vp]
+        lib.orc_eval.restype = ctypes.c_double
+        lib.orc_eval.argtypes = [i, ctypes.c_double, ctypes.c_double, ctypes.c_double, i]
         _ORC = lib
     return _ORC
 
@@ -74,6 +76,11 @@ def set_threads(n):
 
 def max_threads():
     return _orc_lib().orc_max_threads()
+
+
+def kernel_eval(what, d, r, cs=0.0, precision=64):
+    """0: W_r(d); 1: x-component of grad W_r at (d, 0); 2: wall weight Gamma_r(d)."""
+    return _orc_lib().orc_eval(int(what), float(d), float(r), float(cs), int(precision))
 
 
 def grid(pos, ids, origin, cell, dims):

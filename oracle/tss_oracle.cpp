@@ -896,6 +896,24 @@ int orc_max_threads(void) {
 #endif
 }
 
+// Evaluate one kernel function for known-answer tests.  what: 0 = W_s(d),
+// 1 = |grad W_s| along +x at distance d, 2 = wall weight Gamma_s(d) with speed of
+// sound cs; C and G are derived from r as Bind() does.  precision 32 or 64.
+double orc_eval(int what, double d, double r, double cs, int precision) {
+    if (precision == 32) {
+        float rf = float(r), df = float(d);
+        float C = float(20.0 / (14.0 * kPi * double(rf) * double(rf)));
+        float G = float(-120.0 / (14.0 * kPi * double(rf) * double(rf) * double(rf)));
+        if (what == 0) return W<float>(df, rf, C);
+        if (what == 1) return dW<float>({df, 0.f}, df, rf, G).x;
+        return gamma_wall<float>(df, rf, float(cs));
+    }
+    double C = 20.0 / (14.0 * kPi * r * r), G = -120.0 / (14.0 * kPi * r * r * r);
+    if (what == 0) return W<double>(d, r, C);
+    if (what == 1) return dW<double>({d, 0.0}, d, r, G).x;
+    return gamma_wall<double>(d, r, cs);
+}
+
 // Grid build alone (FP32): hash, (cell, id) order and dense cell offsets.
 int orc_grid(int n, const float* pos, const int32_t* id, float ox, float oy, float cell, int dimx, int dimy,
              int32_t* order, int32_t* cell_off) {

@@ -1,0 +1,352 @@
+"""Benchmark: particle-steps/s of the two-scale WCSPH step on the 1M-particle dam break.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A "step" is one WCSPHSolver::AdvanceTS-equivalent step of the whole scene (grids,
+relaxation, densities, forces, splits, integration).  W warm-up steps run first;
+the scene is then reset to its initial state and exactly K steps are timed, each
+bracketed by CUDA events on the launching stream with L2 flushed (a 512 MiB write)
+between steps.  value = sum over the timed steps of the particles processed
+(n_low + n_high at each step) / device time.  e2e repeats the timed run through
+the C ABI with host buffers: the initial state is uploaded from pinned memory and
+every step's particle positions are read back to pinned memory.
+
+With N > 1 (torchrun) every rank runs an independent replica of the scene
+(replicas only: one scene does not shard); value sums the ranks' particle-steps
+over the slowest rank's time.
+
+--impl reference times the CPU restatement of the reference step (the oracle,
+FP32, OpenMP over all host threads) on the same scene; the reference itself is
+CUDA code with an OpenGL front end and has no CPU implementation of its own.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s"
+UNIT = "particle-steps/s"
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes (compulsory own-state traffic per particle; neighbour gathers
+# are served on chip).  Per-particle and per-cell figures per stage.
+# ---------------------------------------------------------------------------
+def stage_bytes(stage, n_low, n_high, c_low, c_high, carry, n_fresh_children):
+    cg = 16 if carry else 0
+    grid = lambda n, c: n * (16 + 24 + 45 + cg) + 12 * c  # keys, scatter, reorder; scan 12 B/cell
+    if stage == "grid_high":
+        return grid(n_high, c_high)
+    if stage == "grid_low":
+        return grid(n_low, c_low)
+    if stage == "relax":
+        return n_fresh_children * 4 * (8 + 8 + 8 + 8 + 16)  # per iteration: R pos,vel,dens/pres; W pos,vel...
+    if stage == "density_high":
+        return n_high * 21 + 4 * c_high
+    if stage == "density_low":
+        return n_low * 21 + 4 * c_low
+    if stage == "force_low":
+        return n_low * (59 + (12 if carry else 0)) + 4 * c_low
+    if stage == "split":
+        return n_low * 1
+    if stage == "force_high":
+        return n_high * (78 + (12 if carry else 0)) + 4 * c_low
+    return 0
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(scene_name, seed, budget_s, threads=None):
+    """The oracle (FP32, the reference's arithmetic) timed on the host cores."""
+    import oracle as O
+    from twoscalesplit_gb300 import scenes
+    if threads:
+        O.set_threads(threads)
+    sc = scenes.make_scene(scene_name, seed=seed)
+    orc = O.Oracle(sc, 32)
+    done, parts, t0 = 0, 0, time.perf_counter()
+    while True:
+        n = orc.get(0, "id").shape[0] + orc.get(1, "id").shape[0]
+        orc.step()
+        done += 1
+        parts += n
+        if time.perf_counter() - t0 >= budget_s or done >= sc.steps:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": parts / dt, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+            "sample": f"{scene_name}: first {done} steps from the initial state ({parts} particle-steps, "
+                      f"{dt:.1f} s), FP32 CPU restatement of the reference step, OpenMP"}
+
+
+def run_reference(args):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    budget = float(os.environ.get("TSS_REF_BUDGET_S", "150"))
+    import oracle as O
+    from twoscalesplit_gb300 import scenes
+    sc = scenes.make_scene(args.scene, seed=0)
+    orc = O.Oracle(sc, 32)
+    for _ in range(min(args.warmup, 1)):
+        orc.step()
+    orc = O.Oracle(sc, 32)
+    t0 = time.perf_counter()
+    parts = 0
+    steps = 0
+    for _ in range(args.steps):
+        parts += orc.get(0, "id").shape[0] + orc.get(1, "id").shape[0]
+        orc.step()
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    v = parts / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.scene, "n_low": sc.n_low, "cap_high": sc.cap_high, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                             "sample": f"{args.scene}: first {steps} of the {args.steps} requested steps from the "
+                                       f"initial state, bounded to {budget:.0f} s"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    from twoscalesplit_gb300 import _abi, build, scenes
+    from twoscalesplit_gb300._abi import TssScaleState, fptr
+    from twoscalesplit_gb300.solver import Solver
+    build.build()
+    sc = scenes.make_scene(args.scene, seed=rank)
+    sol = Solver.from_scene(sc)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    init_low = sol.download(0)
+    empty = {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32), "vel": np.zeros((0, 2), np.float32),
+             "state": np.zeros(0, np.uint8)}
+
+    def reset():
+        sol.upload(0, init_low)
+        sol.upload(1, empty)
+        sol.set_fresh(np.zeros(0, np.int32))
+
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    # warm-up (graph capture happens here)
+    sol.step(max(args.warmup, 1), stream=sh)
+    torch.cuda.synchronize(dev)
+    reset()
+    K = args.steps
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = ClockSampler(local if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    w0 = time.perf_counter()
+    for k in range(K):
+        flush.zero_()
+        evs[k][0].record(stream)
+        sol.step(1, stream=sh)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - w0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    sol.sync()  # raises on a device error (capacity, NaN, timeout)
+    # particles processed per step (deterministic replay, untimed)
+    reset()
+    counts = []
+    for k in range(K):
+        c = sol.counts()
+        counts.append(c["n_low"] + c["n_high"])
+        sol.step(1, stream=sh)
+    c_end = sol.counts()
+    parts = float(sum(counts))
+    # stage times (profiling graph), averaged over a replay of the same steps
+    sol.profile(True)
+    reset()
+    st_sum = {k: 0.0 for k in _abi.STAGE_NAMES}
+    n_prof = min(K, 50)
+    for k in range(n_prof):
+        flush.zero_()
+        sol.step(1, stream=sh)
+        for name, v in sol.stage_times().items():
+            st_sum[name] += v
+    sol.profile(False)
+    st_avg = {k: v / n_prof for k, v in st_sum.items()}
+    # e2e through the C ABI with pinned host buffers
+    reset()
+    sol.step(1, stream=sh)  # keep the graph captured outside the timed region
+    torch.cuda.synchronize(dev)
+    pin_low = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in init_low.items()}
+    cap_h = sc.cap_high
+    out_low = torch.empty((sc.n_low, 2), dtype=torch.float32).pin_memory()
+    out_high = torch.empty((max(cap_h, 1), 2), dtype=torch.float32).pin_memory()
+    lib = sol.lib
+    st_low = TssScaleState(sc.n_low, _abi.iptr(pin_low["id"].numpy()), fptr(pin_low["pos"].numpy()),
+                           fptr(pin_low["vel"].numpy()), _abi.u8ptr(pin_low["state"].numpy()), None, None)
+    import ctypes
+    d2h = 0
+    h2d = sc.n_low * (4 + 8 + 8 + 1)
+    if world > 1:
+        torch.distributed.barrier()
+    e0 = time.perf_counter()
+    _abi.check(lib.tss_solver_upload(sol.h, 0, ctypes.byref(st_low)))
+    sol.upload(1, empty)
+    sol.set_fresh(np.zeros(0, np.int32))
+    for k in range(K):
+        sol.step(1, stream=sh)
+        dl = TssScaleState(sc.n_low, None, fptr(out_low.numpy()), None, None, None, None)
+        _abi.check(lib.tss_solver_download(sol.h, 0, ctypes.byref(dl)))
+        dh = TssScaleState(cap_h, None, fptr(out_high.numpy()), None, None, None, None)
+        _abi.check(lib.tss_solver_download(sol.h, 1, ctypes.byref(dh)))
+        d2h += 8 * (dl.n + dh.n)
+    e2e_s = time.perf_counter() - e0
+    times = torch.tensor([dev_ms, e2e_s, parts], dtype=torch.float64, device=dev)
+    if world > 1:
+        t_max = times.clone()
+        torch.distributed.all_reduce(t_max[:2], op=torch.distributed.ReduceOp.MAX)
+        tot = times.clone()
+        torch.distributed.all_reduce(tot[2:], op=torch.distributed.ReduceOp.SUM)
+        dev_ms, e2e_s, parts_all = float(t_max[0]), float(t_max[1]), float(tot[2])
+    else:
+        parts_all = parts
+    if rank != 0:
+        return
+    value = parts_all / (dev_ms / 1e3)
+    peak, peak_kind = hbm_peak()
+    cfg = sc.config
+    c_low, c_high = cfg.dims_low[0] * cfg.dims_low[1], cfg.dims_high[0] * cfg.dims_high[1]
+    n_high_avg = float(np.mean(counts)) - sc.n_low
+    carry = cfg.relax_iters > 0
+    top = max(st_avg, key=st_avg.get)
+    top_bytes = stage_bytes(top, sc.n_low, n_high_avg, c_low, c_high, carry, 0)
+    top_gbs = top_bytes / (st_avg[top] * 1e-3) / 1e9 if st_avg[top] > 0 else 0.0
+    step_bytes = sum(stage_bytes(s, sc.n_low, n_high_avg, c_low, c_high, carry, 0) for s in _abi.STAGE_NAMES)
+    step_ms = dev_ms / K
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": args.scene, "n_low": sc.n_low, "n_high_end": c_end["n_high"],
+                   "cap_high": sc.cap_high, "dt": cfg.dt, "relax_iters": cfg.relax_iters,
+                   "q1_compat": bool(cfg.flags & 1), "l2": "flushed between timed steps (512 MiB write)",
+                   "parallelism": f"replicas{world}", "seed": 0},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": top_bytes, "launch_ms": st_avg[top],
+                     "step": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (step_ms * 1e-3) / 1e9,
+                              "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak}},
+        "stage_ms": {k: round(v, 5) for k, v in st_avg.items()},
+        "e2e": {"value": parts_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / K,
+                "d2h_bytes_per_step": d2h / K},
+        "gpu_launches": K * (14 + 3 * cfg.relax_iters),  # kernels per step: 2 grids x 4, 5 gathers, finish
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.scene, 0, args.cpu_budget_s)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scene", default="dam_break_1m")
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

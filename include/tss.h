@@ -174,6 +174,18 @@ typedef struct tss_buffers {
 } tss_buffers;
 tss_status tss_solver_device_buffers(tss_solver* s, tss_buffers* out);
 
+/* Stage timing.  With profiling on, the captured step graph also records a CUDA
+ * event at each stage boundary; tss_solver_stage_times then returns the device time
+ * (ms) of each stage of the LAST step (it synchronises).  Stages, in order:
+ *   0 high-res grid, 1 low-res grid, 2 relaxation, 3 high-res density,
+ *   4 low-res density, 5 low-res force + advance + split marks,
+ *   6 split compaction + children, 7 high-res force + integrate + tether.
+ * The reference's CUDA::Timer (CUDA/cuda.h:88-108) was the counterpart; all its
+ * uses are commented out (WCSPHSolver.cu:2653-2676). */
+#define TSS_NUM_STAGES 8
+tss_status tss_solver_profile(tss_solver* s, int enable);
+tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n);
+
 /* Last error message of this handle (NUL-terminated, truncated to len). */
 tss_status tss_solver_last_error(tss_solver* s, char* buf, int len);
 const char* tss_status_string(tss_status st);

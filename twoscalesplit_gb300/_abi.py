@@ -36,6 +36,10 @@ TSS_BUF_ACCEL = 4
 TSS_BUF_SPLIT = 5
 TSS_BUF_WALL_CELL_OFFSET = 6
 
+TSS_NUM_STAGES = 8
+STAGE_NAMES = ["grid_high", "grid_low", "relax", "density_high", "density_low", "force_low", "split",
+               "force_high"]
+
 TSS_ERR_CAPACITY = 0x1
 TSS_ERR_NUMERIC = 0x2
 TSS_ERR_TIMEOUT = 0x4
@@ -157,6 +161,8 @@ def load_library(path=None):
         "tss_solver_copy": (i, [vp, i, i, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "tss_solver_device_buffers": (i, [vp, ctypes.POINTER(TssBuffers)]),
         "tss_solver_last_error": (i, [vp, ctypes.c_char_p, i]),
+        "tss_solver_profile": (i, [vp, i]),
+        "tss_solver_stage_times": (i, [vp, fp, i]),
         "tss_status_string": (ctypes.c_char_p, [i]),
         "tss_grid_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
         "tss_grid_build": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp, ctypes.c_size_t, vp]),

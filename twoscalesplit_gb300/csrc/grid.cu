@@ -1,0 +1,249 @@
+// grid.cu -- counting-sort grid build (see grid.cuh) and the tss_grid_build entry
+// point of the C ABI.
+#include <cuda_runtime.h>
+
+#include "../../include/tss.h"
+#include "grid.cuh"
+
+namespace tss {
+
+int particle_blocks(int cap, int threads) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    long long need = (static_cast<long long>(cap) + threads - 1) / threads;
+    long long lim = static_cast<long long>(sms) * 16;
+    long long b = need < lim ? need : lim;
+    return b < 1 ? 1 : static_cast<int>(b);
+}
+
+__global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restrict__ n_ptr, float ox, float oy,
+                            float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
+                            int* __restrict__ rank) {
+    const int n = *n_ptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int c = cell_hash(pos[i], ox, oy, cell, dimx, dimy);
+        key[i] = c;
+        rank[i] = static_cast<int>(atomicAdd(&count[c], 1u));
+    }
+}
+
+// One tile of kScanTile counts per block, tiles claimed in launch order.
+__global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g, int* tile_ctr, unsigned* err) {
+    __shared__ int s_tile;
+    __shared__ unsigned s_warp[kScanThreads / 32];
+    __shared__ unsigned s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    const int C = g.ncells;
+    const int base = tile * kScanTile + threadIdx.x * kScanItems;
+    unsigned v[kScanItems];
+    if (base + kScanItems <= C) {
+        const uint4* p = reinterpret_cast<const uint4*>(g.count + base);
+        uint4 a = p[0], b = p[1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        uint4* q = reinterpret_cast<uint4*>(g.count + base);
+        q[0] = make_uint4(0, 0, 0, 0);
+        q[1] = make_uint4(0, 0, 0, 0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            int idx = base + k;
+            v[k] = idx < C ? g.count[idx] : 0u;
+            if (idx < C) g.count[idx] = 0u;
+        }
+    }
+    unsigned sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    // block-wide exclusive scan of the per-thread sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+        unsigned wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+        unsigned total = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
+        unsigned prefix = lookback_prefix(g.tile_state, tile, total, err);
+        if (lane == 0) s_prefix = prefix;
+    }
+    __syncthreads();
+    unsigned run = s_prefix + s_warp[warp] + (inc - sum);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int idx = base + k;
+        if (idx < C) g.off[idx] = static_cast<int>(run);
+        run += v[k];
+        if (idx == C - 1) g.off[C] = static_cast<int>(run);
+    }
+    if (C == 0 && tile == 0 && threadIdx.x == 0) g.off[0] = 0;
+}
+
+// Every index below is checked: if a look-back wait gave up (kErrTimeout) the
+// offsets may be inconsistent, and the build then skips entries instead of
+// touching memory outside its buffers.
+__global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
+                               unsigned* err) {
+    const int n = *n_ptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int dst = g.off[g.key[i]] + g.rank[i];
+        if (dst < 0 || dst >= n) {
+            atomicOr(err, kErrTimeout);
+            continue;
+        }
+        g.perm[dst] = make_int2(i, id[i]);
+    }
+}
+
+__global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err) {
+    const int n = *n_ptr;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int2 pe = g.perm[k];
+        const int src = pe.x, id = pe.y;
+        if (src < 0 || src >= n) {
+            atomicOr(err, kErrTimeout);
+            continue;
+        }
+        const int c = g.key[src];
+        const int s = g.off[c], e = g.off[c + 1];
+        if (s < 0 || e > n || s > k || k >= e) {
+            atomicOr(err, kErrTimeout);
+            continue;
+        }
+        int r = 0;
+        for (int j = s; j < e; ++j) r += g.perm[j].y < id;
+        const int dst = s + r;
+        a.dst_pos[dst] = a.src_pos[src];
+        if (a.src_vel) a.dst_vel[dst] = a.src_vel[src];
+        if (a.src_st) {
+            uint8_t st = a.src_st[src];
+            a.dst_st[dst] = st;
+            if (a.h_state0 && (st & 1u) == 0u) *a.h_state0 = 1;
+        }
+        if (a.dst_id) a.dst_id[dst] = id;
+        if (a.src_dens) {
+            a.dst_dens[dst] = a.src_dens[src];
+            a.dst_pres[dst] = a.src_pres[src];
+        }
+        if (a.dst_order) a.dst_order[dst] = src;
+        if (a.slot_map) {
+            if (id >= 0 && id < a.slots) a.slot_map[id] = dst;
+            else atomicOr(err, kErrTimeout);
+        }
+    }
+}
+
+size_t grid_bufs_bytes(int cap, int ncells) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    int ntiles = (ncells + kScanTile - 1) / kScanTile;
+    if (ntiles < 1) ntiles = 1;
+    return al(sizeof(unsigned) * (size_t)ncells) + al(sizeof(int) * ((size_t)ncells + 1)) +
+           al(sizeof(int) * (size_t)cap) * 2 + al(sizeof(int2) * (size_t)cap) +
+           al(sizeof(unsigned long long) * (size_t)ntiles);
+}
+
+GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    char* p = static_cast<char*>(base);
+    GridBufs g;
+    g.ncells = ncells;
+    g.ntiles = (ncells + kScanTile - 1) / kScanTile;
+    if (g.ntiles < 1) g.ntiles = 1;
+    g.count = reinterpret_cast<unsigned*>(p);
+    p += al(sizeof(unsigned) * (size_t)ncells);
+    g.off = reinterpret_cast<int*>(p);
+    p += al(sizeof(int) * ((size_t)ncells + 1));
+    g.key = reinterpret_cast<int*>(p);
+    p += al(sizeof(int) * (size_t)cap);
+    g.rank = reinterpret_cast<int*>(p);
+    p += al(sizeof(int) * (size_t)cap);
+    g.perm = reinterpret_cast<int2*>(p);
+    p += al(sizeof(int2) * (size_t)cap);
+    g.tile_state = reinterpret_cast<unsigned long long*>(p);
+    return g;
+}
+
+cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
+                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, int* tile_ctr,
+                               unsigned* err, cudaStream_t stream) {
+    const int T = 256;
+    const int pb = particle_blocks(cap, T);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(g.tile_state, 0, sizeof(unsigned long long) * g.ntiles, stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(tile_ctr, 0, sizeof(int), stream)) != cudaSuccess) return e;
+    k_grid_keys<<<pb, T, 0, stream>>>(pos, n_ptr, ox, oy, cell, dimx, dimy, g.count, g.key, g.rank);
+    k_grid_scan<<<g.ntiles, kScanThreads, 0, stream>>>(g, tile_ctr, err);
+    k_grid_scatter<<<pb, T, 0, stream>>>(n_ptr, id, g, err);
+    k_grid_reorder<<<pb, T, 0, stream>>>(n_ptr, g, a, err);
+    return cudaGetLastError();
+}
+
+__global__ void k_set_int(int* p, int v) { *p = v; }
+
+}  // namespace tss
+
+// ---------------------------------------------------------------------------
+// C ABI: grid build on caller-owned device memory
+// ---------------------------------------------------------------------------
+namespace {
+// workspace layout: [n + tile counter + error word (256 B)] [grid buffers] [scratch pos copy]
+size_t ws_bytes(int n, int dimx, int dimy) {
+    size_t cells = static_cast<size_t>(dimx) * static_cast<size_t>(dimy);
+    int cap = n > 0 ? n : 1;
+    return 256 + tss::grid_bufs_bytes(cap, static_cast<int>(cells)) + ((sizeof(float2) * (size_t)cap + 255) & ~size_t(255));
+}
+}  // namespace
+
+extern "C" tss_status tss_grid_workspace_size(int n, int dimx, int dimy, size_t* bytes) {
+    if (!bytes || n < 0 || dimx <= 0 || dimy <= 0) return TSS_INVALID_ARG;
+    if (static_cast<long long>(dimx) * dimy >= (1LL << 31) - 1) return TSS_INVALID_ARG;
+    *bytes = ws_bytes(n, dimx, dimy);
+    return TSS_OK;
+}
+
+extern "C" tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, int n, float origin_x, float origin_y,
+                                     float cell_size, int dimx, int dimy, int32_t* d_order, int32_t* d_cell_off,
+                                     void* d_workspace, size_t workspace_bytes, void* stream) {
+    if (n < 0 || dimx <= 0 || dimy <= 0 || !(cell_size > 0.0f) || !d_cell_off || !d_workspace) return TSS_INVALID_ARG;
+    if (n > 0 && (!d_pos || !d_id || !d_order)) return TSS_INVALID_ARG;
+    if (static_cast<long long>(dimx) * dimy >= (1LL << 31) - 1) return TSS_INVALID_ARG;
+    if (workspace_bytes < ws_bytes(n, dimx, dimy)) return TSS_INVALID_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int cells = dimx * dimy;
+    const int cap = n > 0 ? n : 1;
+    char* w = static_cast<char*>(d_workspace);
+    int* n_dev = reinterpret_cast<int*>(w);
+    int* tile_ctr = n_dev + 1;
+    unsigned* err = reinterpret_cast<unsigned*>(n_dev + 2);
+    tss::GridBufs g = tss::grid_bufs_carve(w + 256, cap, cells);
+    g.off = d_cell_off;  // write the offsets straight into the caller's table
+    float2* scratch = reinterpret_cast<float2*>(w + 256 + tss::grid_bufs_bytes(cap, cells));
+    if (cudaMemsetAsync(w, 0, 256, st) != cudaSuccess) return TSS_CUDA_ERROR;
+    if (cudaMemsetAsync(g.count, 0, sizeof(unsigned) * (size_t)cells, st) != cudaSuccess) return TSS_CUDA_ERROR;
+    tss::k_set_int<<<1, 1, 0, st>>>(n_dev, n);
+    tss::ReorderArgs a{};
+    a.src_pos = reinterpret_cast<const float2*>(d_pos);
+    a.dst_pos = scratch;
+    a.dst_order = d_order;
+    cudaError_t e = tss::grid_build_enqueue(reinterpret_cast<const float2*>(d_pos), d_id, n_dev, cap, origin_x, origin_y,
+                                            cell_size, dimx, dimy, g, a, tile_ctr, err, st);
+    return e == cudaSuccess ? TSS_OK : TSS_CUDA_ERROR;
+}

@@ -1,0 +1,77 @@
+// grid.cuh -- uniform-grid neighbour structure on the GPU: a counting sort by cell
+// with a per-cell fix-up into (cell, id) order.
+//
+// Replaces computeParticleHash + thrust::sort_by_key + memset +
+// computeCellStartEndIndices (TwoScale2D/WCSPHSolver.cu:1246-1340, 2814-2854).
+// The grids here have about as many cells as particles, so instead of a radix sort
+// of cell keys the build counts particles per cell, scans the counts (that scan is
+// also the dense cell-offset table the gathers need) and scatters; the order inside
+// a cell is then fixed to ascending id, which makes the result independent of the
+// atomic order and equal to a stable sort by cell of an id-ascending list.
+//
+//   k_grid_keys     key[i] = cell(pos[i]); rank[i] = atomicAdd(&count[cell], 1)
+//   k_grid_scan     off = exclusive_scan(count) in one pass (decoupled look-back);
+//                   count is zeroed for the next build; off[C] = n
+//   k_grid_scatter  perm[off[key[i]] + rank[i]] = (i, id[i])
+//   k_grid_reorder  each sorted slot counts the smaller ids of its cell to find its
+//                   final place and gathers the particle's state there (SoA reorder)
+#pragma once
+#include "tss_device.cuh"
+
+namespace tss {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+struct GridBufs {
+    int ncells;             // C
+    unsigned* count;        // [C], zero between builds
+    int* off;               // [C+1]
+    int* key;               // [cap] cell of list entry i
+    int* rank;              // [cap]
+    int2* perm;             // [cap] (list index, id) in cell order (atomic order inside a cell)
+    unsigned long long* tile_state;  // [ceil(C / kScanTile)]
+    int ntiles;
+};
+
+// What the reorder moves: list-order arrays (src) into sorted-order arrays (dst).
+struct ReorderArgs {
+    const float2* src_pos;
+    const float2* src_vel;     // may be null
+    const uint8_t* src_st;     // may be null
+    const float* src_dens;     // may be null (carried only for the relaxation)
+    const float* src_pres;
+    float2* dst_pos;
+    float2* dst_vel;
+    uint8_t* dst_st;
+    int32_t* dst_id;
+    float* dst_dens;
+    float* dst_pres;
+    int32_t* dst_order;        // may be null: source list index of each sorted position
+    int32_t* slot_map;         // may be null: slot id -> sorted index
+    int slots;                 // size of slot_map
+    int* h_state0;             // may be null: set to 1 if some entry has (state & 1) == 0
+};
+
+__global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restrict__ n_ptr, float ox, float oy,
+                            float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
+                            int* __restrict__ rank);
+__global__ void k_grid_scan(GridBufs g, int* tile_ctr, unsigned* err);
+__global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
+                               unsigned* err);
+__global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err);
+
+// Enqueue a whole build: clears the scan's tile states and `tile_ctr` (a device
+// int), then keys, scan, scatter, reorder.  `n_ptr` is a device int <= cap.
+cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
+                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, int* tile_ctr,
+                               unsigned* err, cudaStream_t stream);
+
+size_t grid_bufs_bytes(int cap, int ncells);
+GridBufs grid_bufs_carve(void* base, int cap, int ncells);
+
+int particle_blocks(int cap, int threads);
+__global__ void k_set_int(int* p, int v);
+
+}  // namespace tss

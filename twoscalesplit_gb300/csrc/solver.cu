@@ -1,0 +1,705 @@
+// solver.cu -- host side of the solver behind the C ABI (include/tss.h).
+//
+// Replaces WCSPHSolver + ParticleSystem's device storage (TwoScale2D/WCSPHSolver.cu:
+// 2287-3238, TwoScale2D/ParticleSystem.cpp:13-119).  Differences by design:
+//  * one device arena per solver, all state resident; no GL interop
+//  * the particle counts stay on the device (no per-step readback, 2760-2781);
+//    every kernel reads its count from device memory
+//  * a whole step is captured once into a CUDA graph and replayed
+//  * all handle state is per handle (the reference kept activeID in a function
+//    static, 2728)
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tss.h"
+#include "grid.cuh"
+#include "sph.cuh"
+
+using namespace tss;
+
+namespace {
+
+struct ScaleBufs {
+    float2 *pos, *vel, *acc, *npos, *nvel;
+    uint8_t *st, *nst;
+    int32_t *id, *nid, *map;
+    float *dens, *pres, *q, *ndens, *npres;
+    GridBufs g;
+};
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Arena {
+    std::vector<std::pair<void**, size_t>> items;
+    template <class T>
+    void add(T** p, size_t count) { items.push_back({reinterpret_cast<void**>(p), al(sizeof(T) * (count ? count : 1))}); }
+    size_t total() const {
+        size_t t = 0;
+        for (auto& it : items) t += it.second;
+        return t;
+    }
+    void carve(char* base) {
+        for (auto& it : items) {
+            *it.first = base;
+            base += it.second;
+        }
+    }
+};
+
+}  // namespace
+
+struct tss_solver {
+    tss_config cfg;
+    Params P;
+    int nL = 0, capH = 0, slotsL = 0, slotsH = 0, nW = 0;
+    int CL = 0, CH = 0;
+    bool carry = false;
+    char* arena = nullptr;
+    ScaleBufs L{}, H{};
+    float2* wpos = nullptr;
+    int* woff = nullptr;
+    Counters* cnt = nullptr;
+    uint8_t* split_flag = nullptr;
+    int32_t* split_ids = nullptr;
+    unsigned long long* split_tiles = nullptr;
+    int split_ntiles = 1;
+    float2* relax_pos = nullptr;
+    float2* relax_vel = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int blocksL = 1, blocksH = 1;
+    bool uploaded[2] = {false, false};  // state replaced since the last step
+    bool profile = false;
+    cudaEvent_t ev[TSS_NUM_STAGES + 1] = {};
+    std::string err;
+
+    tss_status fail(tss_status st, const std::string& msg) {
+        err = msg;
+        return st;
+    }
+    tss_status cuda_fail(cudaError_t e, const char* where) {
+        err = std::string(where) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? TSS_OOM : TSS_CUDA_ERROR;
+    }
+
+    StepView view() const {
+        StepView v{};
+        auto sv = [](const ScaleBufs& b) {
+            ScaleView s{};
+            s.pos = b.pos;
+            s.vel = b.vel;
+            s.st = b.st;
+            s.id = b.id;
+            s.dens = b.dens;
+            s.pres = b.pres;
+            s.q = b.q;
+            s.acc = b.acc;
+            s.off = b.g.off;
+            s.map = b.map;
+            s.npos = b.npos;
+            s.nvel = b.nvel;
+            s.nst = b.nst;
+            s.nid = b.nid;
+            s.ndens = b.ndens;
+            s.npres = b.npres;
+            return s;
+        };
+        v.L = sv(L);
+        v.H = sv(H);
+        if (!carry) {
+            v.L.ndens = v.L.npres = nullptr;
+            v.H.ndens = v.H.npres = nullptr;
+        }
+        v.wpos = wpos;
+        v.woff = woff;
+        v.cnt = cnt;
+        v.split_flag = split_flag;
+        v.split_ids = split_ids;
+        v.split_tiles = split_tiles;
+        v.relax_pos = relax_pos;
+        v.relax_vel = relax_vel;
+        v.nL = nL;
+        return v;
+    }
+
+    ReorderArgs reorder_args(ScaleBufs& b, bool high) {
+        ReorderArgs a{};
+        a.src_pos = b.npos;
+        a.src_vel = b.nvel;
+        a.src_st = b.nst;
+        a.dst_pos = b.pos;
+        a.dst_vel = b.vel;
+        a.dst_st = b.st;
+        a.dst_id = b.id;
+        a.slot_map = b.map;
+        a.slots = high ? slotsH : slotsL;
+        if (carry) {
+            a.src_dens = b.ndens;
+            a.src_pres = b.npres;
+            a.dst_dens = b.dens;
+            a.dst_pres = b.pres;
+        }
+        if (high) a.h_state0 = &cnt->h_state0;
+        return a;
+    }
+
+    // Enqueue one step (the body of AdvanceTS, WCSPHSolver.cu:2726-2810).
+    cudaError_t mark(int k, cudaStream_t s) { return profile ? cudaEventRecord(ev[k], s) : cudaSuccess; }
+
+    cudaError_t enqueue_step(cudaStream_t s) {
+        cudaError_t e;
+        const StepView V = view();
+        if ((e = mark(0, s)) != cudaSuccess) return e;
+        // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid)
+        e = grid_build_enqueue(H.npos, H.nid, &cnt->cur[1], capH, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], H.g,
+                               reorder_args(H, true), &cnt->tile_ctr[0], &cnt->err, s);
+        if (e != cudaSuccess || (e = mark(1, s)) != cudaSuccess) return e;
+        e = grid_build_enqueue(L.npos, L.nid, &cnt->cur[0], nL, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], L.g,
+                               reorder_args(L, false), &cnt->tile_ctr[1], &cnt->err, s);
+        if (e != cudaSuccess || (e = mark(2, s)) != cudaSuccess) return e;
+        // 2. relaxation of last step's children (older snapshot's relaxTransient)
+        for (int it = 0; it < P.relax_iters; ++it) {
+            k_relax_density<<<blocksH, 256, 0, s>>>(P, V);
+            k_relax_force<<<blocksH, 256, 0, s>>>(P, V);
+            k_relax_apply<<<blocksH, 256, 0, s>>>(P, V);
+        }
+        if ((e = mark(3, s)) != cudaSuccess) return e;
+        // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
+        k_density_high<<<blocksH, 256, 0, s>>>(P, V);
+        if ((e = mark(4, s)) != cudaSuccess) return e;
+        k_density_low<<<blocksL, 256, 0, s>>>(P, V);
+        if ((e = mark(5, s)) != cudaSuccess) return e;
+        k_force_low<<<blocksL, 256, 0, s>>>(P, V);
+        if ((e = mark(6, s)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(split_tiles, 0, sizeof(unsigned long long) * split_ntiles, s)) != cudaSuccess)
+            return e;
+        k_split<<<split_ntiles, kSplitThreads, 0, s>>>(P, V);
+        if ((e = mark(7, s)) != cudaSuccess) return e;
+        k_force_high<<<blocksH, 256, 0, s>>>(P, V);
+        k_step_finish<<<1, 32, 0, s>>>(cnt);
+        if ((e = mark(8, s)) != cudaSuccess) return e;
+        return cudaGetLastError();
+    }
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+
+    ~tss_solver() {
+        drop_graph();
+        for (auto& x : ev)
+            if (x) cudaEventDestroy(x);
+        if (stream) cudaStreamDestroy(stream);
+        if (arena) cudaFree(arena);
+    }
+};
+
+namespace {
+
+__global__ void k_iota(int32_t* p, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+__global__ void k_fill_i32(int32_t* p, int n, int v) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_set_counts(Counters* c, int nL, int nH) {
+    c->cur[0] = c->next[0] = nL;
+    c->cur[1] = c->next[1] = nH;
+    c->h_state0 = 0;
+    for (int k = 0; k < 8; ++k) c->tile_ctr[k] = 0;
+}
+__global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
+
+bool finite_cfg(const tss_config* c) {
+    const float v[] = {c->domain_origin[0], c->domain_origin[1], c->domain_end[0], c->domain_end[1], c->r_low,
+                       c->r_high, c->rest_density, c->tait_b, c->speed_sound, c->alpha, c->tension, c->dt,
+                       c->gravity, c->relax_dt_div};
+    for (float x : v)
+        if (!std::isfinite(x)) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tss_status_string(tss_status st) {
+    switch (st) {
+        case TSS_OK: return "ok";
+        case TSS_INVALID_ARG: return "invalid argument";
+        case TSS_OOM: return "out of memory";
+        case TSS_CUDA_ERROR: return "CUDA error";
+        case TSS_CAPACITY: return "particle pool capacity exceeded";
+        case TSS_NUMERIC: return "NaN or Inf in the particle state";
+        case TSS_TIMEOUT: return "device-side wait timed out";
+        case TSS_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+tss_status tss_config_init(tss_config* cfg, float xs, float ys, float xe, float ye, float effective_radius,
+                           float effective_radius_high, float rest_density, float tait_coeff, float speed_sound,
+                           float alpha, float tension_coefficient, float time_step) {
+    if (!cfg) return TSS_INVALID_ARG;
+    if (xs >= xe || ys >= ye) return TSS_INVALID_ARG;  // WCSPHConfig ctor, 2312-2316
+    if (!(effective_radius > 0.0f) || !(effective_radius_high > 0.0f)) return TSS_INVALID_ARG;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->domain_origin[0] = xs;
+    cfg->domain_origin[1] = ys;
+    cfg->domain_end[0] = xe;
+    cfg->domain_end[1] = ye;
+    cfg->dims_low[0] = static_cast<int>(std::ceil((xe - xs) / effective_radius));
+    cfg->dims_low[1] = static_cast<int>(std::ceil((ye - ys) / effective_radius));
+    cfg->dims_high[0] = static_cast<int>(std::ceil((xe - xs) / effective_radius_high));
+    cfg->dims_high[1] = static_cast<int>(std::ceil((ye - ys) / effective_radius_high));
+    cfg->r_low = effective_radius;
+    cfg->r_high = effective_radius_high;
+    cfg->rest_density = rest_density;
+    cfg->tait_b = tait_coeff;
+    cfg->speed_sound = speed_sound;
+    cfg->alpha = alpha;
+    cfg->tension = tension_coefficient;
+    cfg->dt = time_step;
+    cfg->gravity = 9.81f;
+    cfg->roi[0] = 0.5f;
+    cfg->roi[1] = -INFINITY;
+    cfg->roi[2] = INFINITY;
+    cfg->roi[3] = INFINITY;
+    cfg->relax_iters = 0;
+    cfg->relax_dt_div = 10.0f;
+    cfg->flags = TSS_FLAG_Q1_COMPAT;
+    return TSS_OK;
+}
+
+tss_status tss_solver_create(const tss_config* cfg, int n_low, const float* low_pos, const float* low_vel,
+                             float mass_low, int cap_high, float mass_high, int n_wall, const float* wall_pos,
+                             float mass_wall, tss_solver** out) {
+    if (!out || !cfg) return TSS_INVALID_ARG;
+    *out = nullptr;
+    if (n_low < 0 || cap_high < 0 || n_wall < 0) return TSS_INVALID_ARG;
+    if ((n_low > 0 && !low_pos) || (n_wall > 0 && !wall_pos)) return TSS_INVALID_ARG;
+    if (!finite_cfg(cfg) || cfg->dims_low[0] <= 0 || cfg->dims_low[1] <= 0 || cfg->dims_high[0] <= 0 ||
+        cfg->dims_high[1] <= 0 || !(cfg->r_low > 0) || !(cfg->r_high > 0) || cfg->relax_iters < 0 ||
+        cfg->relax_iters > 64 || !(cfg->relax_dt_div > 0))
+        return TSS_INVALID_ARG;
+    if (static_cast<long long>(cfg->dims_low[0]) * cfg->dims_low[1] >= (1LL << 31) - 1 ||
+        static_cast<long long>(cfg->dims_high[0]) * cfg->dims_high[1] >= (1LL << 31) - 1)
+        return TSS_INVALID_ARG;
+    if (static_cast<long long>(n_low) * 4 >= (1LL << 31) - 1) return TSS_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return TSS_NO_DEVICE;
+
+    tss_solver* s = new (std::nothrow) tss_solver();
+    if (!s) return TSS_OOM;
+    s->cfg = *cfg;
+    s->nL = n_low;
+    s->capH = cap_high;
+    s->slotsL = n_low;
+    s->slotsH = 4 * n_low;
+    s->nW = n_wall;
+    s->CL = cfg->dims_low[0] * cfg->dims_low[1];
+    s->CH = cfg->dims_high[0] * cfg->dims_high[1];
+    s->carry = cfg->relax_iters > 0;
+    Params& P = s->P;
+    P.ox = cfg->domain_origin[0];
+    P.oy = cfg->domain_origin[1];
+    P.dimL[0] = cfg->dims_low[0];
+    P.dimL[1] = cfg->dims_low[1];
+    P.dimH[0] = cfg->dims_high[0];
+    P.dimH[1] = cfg->dims_high[1];
+    P.r = cfg->r_low;
+    P.rh = cfg->r_high;
+    P.rho0 = cfg->rest_density;
+    P.B = cfg->tait_b;
+    P.cs = cfg->speed_sound;
+    P.alpha = cfg->alpha;
+    P.sigma = cfg->tension;
+    P.dt = cfg->dt;
+    P.g = cfg->gravity;
+    const double r = cfg->r_low, rh = cfg->r_high;  // Bind(), 2559-2590
+    P.CL = static_cast<float>(20.0 / (14.0 * kPi * r * r));
+    P.GL = static_cast<float>(-120.0 / (14.0 * kPi * r * r * r));
+    P.CH = static_cast<float>(20.0 / (14.0 * kPi * rh * rh));
+    P.GH = static_cast<float>(-120.0 / (14.0 * kPi * rh * rh * rh));
+    P.mL = mass_low;
+    P.mH = mass_high;
+    P.mB = mass_wall;
+    P.cBL = mass_wall / (mass_low + mass_wall);
+    P.cBH = mass_wall / (mass_high + mass_wall);
+    P.hx = (cfg->r_low + cfg->r_high) / 2.0f;
+    P.relax_dt = cfg->dt / cfg->relax_dt_div;
+    for (int k = 0; k < 4; ++k) P.roi[k] = cfg->roi[k];
+    P.relax_iters = cfg->relax_iters;
+    P.q1 = (cfg->flags & TSS_FLAG_Q1_COMPAT) ? 1 : 0;
+    P.slotsL = s->slotsL;
+    P.slotsH = s->slotsH;
+    P.capH = cap_high;
+
+    // ---- one arena for everything ----
+    Arena A;
+    auto scale = [&](ScaleBufs& b, int cap, int slots, int cells) {
+        A.add(&b.pos, cap);
+        A.add(&b.vel, cap);
+        A.add(&b.acc, cap);
+        A.add(&b.npos, cap);
+        A.add(&b.nvel, cap);
+        A.add(&b.st, cap);
+        A.add(&b.nst, cap);
+        A.add(&b.id, cap);
+        A.add(&b.nid, cap);
+        A.add(&b.map, slots);
+        A.add(&b.dens, cap);
+        A.add(&b.pres, cap);
+        A.add(&b.q, cap);
+        A.add(&b.ndens, s->carry ? cap : 1);
+        A.add(&b.npres, s->carry ? cap : 1);
+        (void)cells;
+    };
+    scale(s->L, n_low, s->slotsL, s->CL);
+    scale(s->H, cap_high, s->slotsH, s->CH);
+    char* gL = nullptr;
+    char* gH = nullptr;
+    char* gW = nullptr;
+    A.add(&gL, grid_bufs_bytes(n_low > 0 ? n_low : 1, s->CL));
+    A.add(&gH, grid_bufs_bytes(cap_high > 0 ? cap_high : 1, s->CH));
+    A.add(&gW, grid_bufs_bytes(n_wall > 0 ? n_wall : 1, s->CL));
+    float2* wraw = nullptr;
+    int32_t* wid = nullptr;
+    A.add(&s->wpos, n_wall);
+    A.add(&wraw, n_wall);
+    A.add(&wid, n_wall);
+    A.add(&s->cnt, 1);
+    int* nW_dev = nullptr;
+    A.add(&nW_dev, 4);
+    A.add(&s->split_flag, n_low);
+    A.add(&s->split_ids, n_low);
+    s->split_ntiles = n_low > 0 ? (n_low + kSplitTile - 1) / kSplitTile : 1;
+    A.add(&s->split_tiles, s->split_ntiles);
+    A.add(&s->relax_pos, s->carry ? cap_high : 1);
+    A.add(&s->relax_vel, s->carry ? cap_high : 1);
+    cudaError_t e = cudaMalloc(&s->arena, A.total());
+    if (e != cudaSuccess) {
+        tss_status st = e == cudaErrorMemoryAllocation ? TSS_OOM : TSS_CUDA_ERROR;
+        delete s;
+        return st;
+    }
+    A.carve(s->arena);
+    s->L.g = grid_bufs_carve(gL, n_low > 0 ? n_low : 1, s->CL);
+    s->H.g = grid_bufs_carve(gH, cap_high > 0 ? cap_high : 1, s->CH);
+    GridBufs gw = grid_bufs_carve(gW, n_wall > 0 ? n_wall : 1, s->CL);
+    s->woff = gw.off;
+    s->blocksL = particle_blocks(n_low > 0 ? n_low : 1, 256);
+    s->blocksH = particle_blocks(cap_high > 0 ? cap_high : 1, 256);
+
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete s;
+        return TSS_CUDA_ERROR;
+    }
+    cudaStream_t st = s->stream;
+    // zero the whole arena: counts, maps (set to -1 below), pools
+    e = cudaMemsetAsync(s->arena, 0, A.total(), st);
+    if (e == cudaSuccess && s->slotsL > 0) k_fill_i32<<<particle_blocks(s->slotsL, 256), 256, 0, st>>>(s->L.map, s->slotsL, -1);
+    if (e == cudaSuccess && s->slotsH > 0) k_fill_i32<<<particle_blocks(s->slotsH, 256), 256, 0, st>>>(s->H.map, s->slotsH, -1);
+    if (e == cudaSuccess && n_low > 0) {
+        e = cudaMemcpyAsync(s->L.npos, low_pos, sizeof(float2) * n_low, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && low_vel)
+            e = cudaMemcpyAsync(s->L.nvel, low_vel, sizeof(float2) * n_low, cudaMemcpyHostToDevice, st);
+        k_iota<<<particle_blocks(n_low, 256), 256, 0, st>>>(s->L.nid, n_low);
+    }
+    k_set_counts<<<1, 1, 0, st>>>(s->cnt, n_low, 0);
+    // boundary grid, once (initBoundaries, 3205-3238): iota ids, low grid
+    if (e == cudaSuccess && n_wall > 0) {
+        e = cudaMemcpyAsync(wraw, wall_pos, sizeof(float2) * n_wall, cudaMemcpyHostToDevice, st);
+        k_iota<<<particle_blocks(n_wall, 256), 256, 0, st>>>(wid, n_wall);
+        k_set_int<<<1, 1, 0, st>>>(nW_dev, n_wall);
+        ReorderArgs a{};
+        a.src_pos = wraw;
+        a.dst_pos = s->wpos;
+        if (e == cudaSuccess)
+            e = grid_build_enqueue(wraw, wid, nW_dev, n_wall, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], gw, a,
+                                   &s->cnt->tile_ctr[2], &s->cnt->err, st);
+    } else if (e == cudaSuccess) {
+        // no walls: offsets all zero (already zeroed)
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        tss_status ret = e == cudaErrorMemoryAllocation ? TSS_OOM : TSS_CUDA_ERROR;
+        delete s;
+        return ret;
+    }
+    *out = s;
+    return TSS_OK;
+}
+
+void tss_solver_destroy(tss_solver* s) { delete s; }
+
+tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
+    if (!s || n_steps < 0) return TSS_INVALID_ARG;
+    if (n_steps == 0) return TSS_OK;
+    cudaError_t e;
+    if (!s->exec) {
+        cudaStream_t cap = s->stream;
+        if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return s->cuda_fail(e, "begin capture");
+        cudaError_t e1 = s->enqueue_step(cap);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(cap, &g);
+        if (e1 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return s->cuda_fail(e1, "enqueue step");
+        }
+        if (e != cudaSuccess) return s->cuda_fail(e, "end capture");
+        s->graph = g;
+        if ((e = cudaGraphInstantiate(&s->exec, g, 0)) != cudaSuccess) {
+            s->drop_graph();
+            return s->cuda_fail(e, "instantiate");
+        }
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    for (int k = 0; k < n_steps; ++k)
+        if ((e = cudaGraphLaunch(s->exec, st)) != cudaSuccess) return s->cuda_fail(e, "graph launch");
+    s->uploaded[0] = s->uploaded[1] = false;
+    return TSS_OK;
+}
+
+tss_status tss_solver_sync(tss_solver* s) {
+    if (!s) return TSS_INVALID_ARG;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return s->cuda_fail(e, "synchronize");
+    Counters c;
+    if ((e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return s->cuda_fail(e, "read counters");
+    if (c.err & kErrTimeout) return s->fail(TSS_TIMEOUT, "a device-side look-back wait gave up");
+    if (c.err & kErrCapacity) return s->fail(TSS_CAPACITY, "high-res pool capacity exceeded by a split");
+    if (c.err & kErrNumeric) return s->fail(TSS_NUMERIC, "NaN/Inf density, pressure or acceleration");
+    return TSS_OK;
+}
+
+tss_status tss_solver_counts(tss_solver* s, tss_counts* out) {
+    if (!s || !out) return TSS_INVALID_ARG;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    Counters c;
+    if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cuda_fail(e, "counts");
+    out->n_low = c.cur[0];
+    out->n_high = c.cur[1];
+    out->n_transient_low = c.cur[1] / 4;
+    out->n_split_last = c.n_split;
+    out->steps = c.steps;
+    out->error_bits = c.err;
+    return TSS_OK;
+}
+
+tss_status tss_solver_download(tss_solver* s, int scale, tss_scale_state* out) {
+    if (!s || !out || (scale != 0 && scale != 1)) return TSS_INVALID_ARG;
+    tss_counts c;
+    tss_status st = tss_solver_counts(s, &c);
+    if (st != TSS_OK) return st;
+    const int n = scale == 0 ? c.n_low : c.n_high;
+    ScaleBufs& b = scale == 0 ? s->L : s->H;
+    if (out->n < n) {
+        out->n = n;
+        return s->fail(TSS_INVALID_ARG, "download buffer too small");
+    }
+    out->n = n;
+    if (n == 0) return TSS_OK;
+    cudaError_t e = cudaSuccess;
+    if (out->id) e = cudaMemcpy(out->id, b.nid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && out->pos) e = cudaMemcpy(out->pos, b.npos, sizeof(float2) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && out->vel) e = cudaMemcpy(out->vel, b.nvel, sizeof(float2) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && out->state) e = cudaMemcpy(out->state, b.nst, n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && (out->dens || out->pres)) {
+        if (s->carry) {
+            if (out->dens) e = cudaMemcpy(out->dens, b.ndens, sizeof(float) * n, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && out->pres) e = cudaMemcpy(out->pres, b.npres, sizeof(float) * n, cudaMemcpyDeviceToHost);
+        } else {
+            // list order = last step's sorted order for the particles that existed then
+            Counters cc;
+            e = cudaMemcpy(&cc, s->cnt, sizeof(cc), cudaMemcpyDeviceToHost);
+            int m = (cc.steps > 0 && !s->uploaded[scale]) ? cc.sorted[scale] : 0;
+            if (m > n) m = n;
+            if (out->dens) {
+                std::memset(out->dens, 0, sizeof(float) * n);
+                if (e == cudaSuccess && m) e = cudaMemcpy(out->dens, b.dens, sizeof(float) * m, cudaMemcpyDeviceToHost);
+            }
+            if (out->pres) {
+                std::memset(out->pres, 0, sizeof(float) * n);
+                if (e == cudaSuccess && m) e = cudaMemcpy(out->pres, b.pres, sizeof(float) * m, cudaMemcpyDeviceToHost);
+            }
+        }
+    }
+    if (e != cudaSuccess) return s->cuda_fail(e, "download");
+    return TSS_OK;
+}
+
+tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in) {
+    if (!s || !in || (scale != 0 && scale != 1)) return TSS_INVALID_ARG;
+    const int n = in->n;
+    const int cap = scale == 0 ? s->nL : s->capH;
+    const int slots = scale == 0 ? s->slotsL : s->slotsH;
+    if (n < 0 || n > cap) return s->fail(TSS_INVALID_ARG, "count exceeds capacity");
+    if (scale == 0 && n != s->nL) return s->fail(TSS_INVALID_ARG, "the low-res count is fixed at creation");
+    if (n > 0 && (!in->id || !in->pos || !in->state)) return s->fail(TSS_INVALID_ARG, "missing arrays");
+    std::vector<char> seen(static_cast<size_t>(slots), 0);
+    for (int i = 0; i < n; ++i) {
+        const int id = in->id[i];
+        if (id < 0 || id >= slots || seen[id]) return s->fail(TSS_INVALID_ARG, "ids must be unique and in range");
+        seen[id] = 1;
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    ScaleBufs& b = scale == 0 ? s->L : s->H;
+    if (e == cudaSuccess && n > 0) {
+        e = cudaMemcpy(b.nid, in->id, sizeof(int32_t) * n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(b.npos, in->pos, sizeof(float2) * n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            if (in->vel) e = cudaMemcpy(b.nvel, in->vel, sizeof(float2) * n, cudaMemcpyHostToDevice);
+            else e = cudaMemset(b.nvel, 0, sizeof(float2) * n);
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(b.nst, in->state, n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && s->carry) {
+            if (in->dens) e = cudaMemcpy(b.ndens, in->dens, sizeof(float) * n, cudaMemcpyHostToDevice);
+            else e = cudaMemset(b.ndens, 0, sizeof(float) * n);
+            if (e == cudaSuccess) {
+                if (in->pres) e = cudaMemcpy(b.npres, in->pres, sizeof(float) * n, cudaMemcpyHostToDevice);
+                else e = cudaMemset(b.npres, 0, sizeof(float) * n);
+            }
+        }
+    }
+    if (e == cudaSuccess && slots > 0) {
+        k_fill_i32<<<particle_blocks(slots, 256), 256, 0, s->stream>>>(b.map, slots, -1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        Counters c;
+        e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) {
+            int nL = scale == 0 ? n : c.cur[0];
+            int nH = scale == 1 ? n : c.cur[1];
+            k_set_counts<<<1, 1, 0, s->stream>>>(s->cnt, nL, nH);
+            e = cudaStreamSynchronize(s->stream);
+        }
+    }
+    if (e != cudaSuccess) return s->cuda_fail(e, "upload");
+    s->uploaded[scale] = true;
+    return TSS_OK;
+}
+
+tss_status tss_solver_get_fresh(tss_solver* s, int* n, int32_t* parents) {
+    if (!s || !n) return TSS_INVALID_ARG;
+    Counters c;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && parents && c.n_fresh > 0)
+        e = cudaMemcpy(parents, s->split_ids, sizeof(int32_t) * c.n_fresh, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cuda_fail(e, "get fresh");
+    *n = c.n_fresh;
+    return TSS_OK;
+}
+
+tss_status tss_solver_set_fresh(tss_solver* s, int n, const int32_t* parents) {
+    if (!s || n < 0 || n > s->nL || (n > 0 && !parents)) return TSS_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        if (parents[i] < 0 || parents[i] >= s->slotsL) return s->fail(TSS_INVALID_ARG, "parent id out of range");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && n > 0) e = cudaMemcpy(s->split_ids, parents, sizeof(int32_t) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_set_fresh<<<1, 1, 0, s->stream>>>(s->cnt, n);
+        e = cudaStreamSynchronize(s->stream);
+    }
+    if (e != cudaSuccess) return s->cuda_fail(e, "set fresh");
+    return TSS_OK;
+}
+
+tss_status tss_solver_copy(tss_solver* s, int scale, int which, void* dst, size_t count, size_t* written) {
+    if (!s || (scale != 0 && scale != 1)) return TSS_INVALID_ARG;
+    Counters c;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cuda_fail(e, "copy");
+    ScaleBufs& b = scale == 0 ? s->L : s->H;
+    // particles sorted in the last step: the count before its splits
+    const int n_sorted = c.steps > 0 ? c.sorted[scale] : 0;
+    const void* src = nullptr;
+    size_t n = 0, esz = 4;
+    switch (which) {
+        case TSS_BUF_SORTED_ID: src = b.id; n = n_sorted; break;
+        case TSS_BUF_CELL_OFFSET: src = b.g.off; n = static_cast<size_t>(b.g.ncells) + 1; break;
+        case TSS_BUF_DENSITY: src = b.dens; n = n_sorted; break;
+        case TSS_BUF_PRESSURE: src = b.pres; n = n_sorted; break;
+        case TSS_BUF_ACCEL: src = b.acc; n = 2 * static_cast<size_t>(n_sorted); break;
+        case TSS_BUF_SPLIT:
+            if (scale != 0) return TSS_INVALID_ARG;
+            src = s->split_ids;
+            n = c.n_split;
+            break;
+        case TSS_BUF_WALL_CELL_OFFSET:
+            if (scale != 0) return TSS_INVALID_ARG;
+            src = s->woff;
+            n = static_cast<size_t>(s->CL) + 1;
+            break;
+        default: return TSS_INVALID_ARG;
+    }
+    if (written) *written = n;
+    if (!dst) return TSS_OK;
+    if (count < n) return s->fail(TSS_INVALID_ARG, "destination too small");
+    if (n && (e = cudaMemcpy(dst, src, n * esz, cudaMemcpyDeviceToHost)) != cudaSuccess) return s->cuda_fail(e, "copy");
+    return TSS_OK;
+}
+
+tss_status tss_solver_device_buffers(tss_solver* s, tss_buffers* out) {
+    if (!s || !out) return TSS_INVALID_ARG;
+    const ScaleBufs* b[2] = {&s->L, &s->H};
+    for (int k = 0; k < 2; ++k) {
+        out->pos[k] = reinterpret_cast<const float*>(b[k]->npos);
+        out->vel[k] = reinterpret_cast<const float*>(b[k]->nvel);
+        out->dens[k] = b[k]->dens;
+        out->id[k] = b[k]->nid;
+        out->state[k] = b[k]->nst;
+    }
+    out->counts = reinterpret_cast<const int*>(reinterpret_cast<const char*>(s->cnt) + offsetof(Counters, cur));
+    return TSS_OK;
+}
+
+tss_status tss_solver_profile(tss_solver* s, int enable) {
+    if (!s) return TSS_INVALID_ARG;
+    const bool want = enable != 0;
+    if (want == s->profile) return TSS_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return s->cuda_fail(e, "profile");
+    if (want)
+        for (auto& x : s->ev)
+            if (!x && (e = cudaEventCreate(&x)) != cudaSuccess) return s->cuda_fail(e, "event create");
+    s->profile = want;
+    s->drop_graph();  // re-captured with (or without) the event nodes at the next step
+    return TSS_OK;
+}
+
+tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n) {
+    if (!s || !ms || n < TSS_NUM_STAGES) return TSS_INVALID_ARG;
+    if (!s->profile) return s->fail(TSS_INVALID_ARG, "profiling is off");
+    cudaError_t e = cudaDeviceSynchronize();
+    for (int k = 0; k < TSS_NUM_STAGES && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&ms[k], s->ev[k], s->ev[k + 1]);
+    if (e != cudaSuccess) return s->cuda_fail(e, "stage times");
+    return TSS_OK;
+}
+
+tss_status tss_solver_last_error(tss_solver* s, char* buf, int len) {
+    if (!s || !buf || len <= 0) return TSS_INVALID_ARG;
+    std::snprintf(buf, static_cast<size_t>(len), "%s", s->err.c_str());
+    return TSS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,557 @@
+// sph.cu -- density, force, split and relaxation kernels of the two-scale step.
+//
+// One thread per particle in (cell, id) order.  Because the arrays are sorted by
+// cell, the candidates of one row of the 3x3 (or wider cross-scale) cell window are
+// one contiguous span [off[row + cx0], off[row + cx1 + 1]), and consecutive threads
+// of a warp walk overlapping spans, so neighbour loads are coalesced and served from
+// L1.  Each thread sums its candidates in the reference's order (cells row by row,
+// particles in cell order), which keeps every FP32 sum identical to the reference's
+// for the same list order.
+#include "sph.cuh"
+
+namespace tss {
+
+namespace {
+__device__ __forceinline__ int nthreads() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ int tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_density_high(Params P, StepView V) {
+    const int n = V.cnt->cur[1];
+    const ScaleView& H = V.H;
+    const ScaleView& L = V.L;
+    for (int i = tid(); i < n; i += nthreads()) {
+        const float2 p = H.pos[i];
+        const unsigned s = H.st[i];
+        float d = 0.0f, dl = 0.0f;
+        int csx, csy, cex, cey;
+        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimH[0];
+            const int b = H.off[row + cex + 1];
+            for (int j = H.off[row + csx]; j < b; ++j) {
+                if (!lamHH(s, H.st[j])) continue;
+                float dist = vnorm(sub(p, H.pos[j]));
+                if (dist <= P.rh) d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            }
+        }
+        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = L.off[row + cex + 1];
+            if (P.q1) {
+                // The reference reads the HIGH sorted list at LOW-grid ranges; past
+                // n_high that list still holds its initial identity (slot t at t).
+                for (int t = L.off[row + csx]; t < b; ++t) {
+                    float2 pj = make_float2(0.0f, 0.0f);
+                    unsigned sj = 0;
+                    if (t < n) {
+                        pj = H.pos[t];
+                        sj = H.st[t];
+                    } else {
+                        int k = t < P.slotsH ? H.map[t] : -1;
+                        if (k >= 0) {
+                            pj = H.pos[k];
+                            sj = H.st[k];
+                        }
+                    }
+                    if (!lamHL(s, sj)) continue;
+                    float dist = vnorm(sub(p, pj));
+                    if (dist <= P.rh) d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                }
+            } else {
+                for (int t = L.off[row + csx]; t < b; ++t) {
+                    if (!lamHL(s, L.st[t])) continue;
+                    float dist = vnorm(sub(p, L.pos[t]));
+                    if (dist <= P.rh) dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                }
+            }
+        }
+        d *= P.mH;
+        dl *= P.mL;
+        d += dl;
+        const float pr = tait(d, P);
+        H.dens[i] = d;
+        H.pres[i] = pr;
+        H.q[i] = pr / (d * d);
+        if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Low-res density + Tait, computeParticleDensityPressure (WCSPHSolver.cu:1342-1424)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_density_low(Params P, StepView V) {
+    const int n = V.cnt->cur[0];
+    const ScaleView& H = V.H;
+    const ScaleView& L = V.L;
+    const bool cross = V.cnt->h_state0 != 0;  // only state-0 high-res particles can contribute
+    for (int i = tid(); i < n; i += nthreads()) {
+        const float2 p = L.pos[i];
+        const unsigned s = L.st[i];
+        float d = 0.0f, dh = 0.0f;
+        int csx, csy, cex, cey;
+        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = L.off[row + cex + 1];
+            for (int j = L.off[row + csx]; j < b; ++j) {
+                float dist = vnorm(sub(p, L.pos[j]));
+                if (dist <= P.r) d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            }
+        }
+        if (cross) {
+            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+            for (int cy = csy; cy <= cey; ++cy) {
+                const int row = cy * P.dimH[0];
+                const int b = H.off[row + cex + 1];
+                for (int j = H.off[row + csx]; j < b; ++j) {
+                    if (!lamLH(s, H.st[j])) continue;
+                    float dist = vnorm(sub(p, H.pos[j]));
+                    if (dist <= P.r) dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                }
+            }
+        }
+        d *= P.mL;
+        dh *= P.mH;
+        const float rho = d + dh;
+        const float pr = tait(rho, P);
+        L.dens[i] = rho;
+        L.pres[i] = pr;
+        L.q[i] = pr / (rho * rho);
+        if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Low-res force + advance + split test: computeParticleAcceleration
+// (WCSPHSolver.cu:1648-1865) with advance (1604-1646) fused; its predicted position
+// is the advanced position bit for bit.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_force_low(Params P, StepView V) {
+    const int n = V.cnt->cur[0];
+    const ScaleView& H = V.H;
+    const ScaleView& L = V.L;
+    const bool cross = V.cnt->h_state0 != 0;
+    for (int i = tid(); i < n; i += nthreads()) {
+        float2 p = L.pos[i], v = L.vel[i];
+        const unsigned s = L.st[i];
+        const float dens = L.dens[i], qi = L.q[i];
+        float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f);
+        float2 accT = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
+        int csx, csy, cex, cey;
+        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = L.off[row + cex + 1];
+            for (int j = L.off[row + csx]; j < b; ++j) {
+                const float2 pij = sub(p, L.pos[j]);
+                const float dist = vnorm(pij);
+                if (dist != 0.0f && dist < P.r) {
+                    if (!notDeleted(L.st[j])) continue;
+                    pair_force(P, pij, dist, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
+                }
+            }
+            const int wb = V.woff[row + cex + 1];
+            for (int k = V.woff[row + csx]; k < wb; ++k) {
+                const float2 pik = sub(p, V.wpos[k]);
+                const float gm = wall_weight(vnorm(pik), P.r, P.cs);
+                accB.x += P.cBL * gm * pik.x;
+                accB.y += P.cBL * gm * pik.y;
+            }
+        }
+        if (cross) {
+            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+            for (int cy = csy; cy <= cey; ++cy) {
+                const int row = cy * P.dimH[0];
+                const int b = H.off[row + cex + 1];
+                for (int j = H.off[row + csx]; j < b; ++j) {
+                    if (!lamLH(s, H.st[j])) continue;
+                    const float2 pij = sub(p, H.pos[j]);
+                    const float dist = vnorm(pij);
+                    if (dist != 0.0f && dist < P.r)
+                        pair_force(P, pij, dist, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
+                }
+            }
+        }
+        acc.x *= -P.mL;
+        acc.y *= -P.mL;
+        accH.x *= -P.mH;
+        accH.y *= -P.mH;
+        acc.x += accH.x;
+        acc.y += accH.y;
+        acc.x -= P.sigma * accT.x;
+        acc.y -= P.sigma * accT.y;
+        acc.x += accB.x;
+        acc.y += accB.y;
+        acc.y -= P.g;
+        L.acc[i] = acc;
+        if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+        v.x += P.dt * acc.x;
+        v.y += P.dt * acc.y;
+        p.x += P.dt * v.x;
+        p.y += P.dt * v.y;
+        L.npos[i] = p;
+        L.nvel[i] = v;
+        L.nid[i] = L.id[i];
+        uint8_t ns = static_cast<uint8_t>(s);
+        uint8_t flag = 0;
+        if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
+            ns = 1;
+            flag = 1;
+        }
+        L.nst[i] = ns;
+        V.split_flag[i] = flag;
+        if (L.ndens) {
+            L.ndens[i] = dens;
+            L.npres[i] = L.pres[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Ordered stream compaction of the split flags (warp ballot + block scan +
+// decoupled look-back) and creation of the 4 children of each split
+// (initSubParticlesAndAddToList, WCSPHSolver.cu:956-1005): children of the k-th
+// split parent (in sorted order) take high-res list entries n_high + 4k + 0..3.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
+    __shared__ int s_tile;
+    __shared__ unsigned s_warp[kSplitThreads / 32];
+    __shared__ unsigned s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&V.cnt->tile_ctr[7], 1);
+    __syncthreads();
+    const int tile = s_tile;
+    const int n = V.cnt->cur[0];
+    const int nH = V.cnt->cur[1];
+    const int ntiles = max(1, (n + kSplitTile - 1) / kSplitTile);
+    if (tile >= ntiles) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // warp-striped items: item k of lane l of warp w is tile base + (w*K + k)*32 + l,
+    // so each warp's ballots cover 32 consecutive particles in order
+    const int wbase = tile * kSplitTile + warp * kSplitItems * 32;
+    unsigned warp_count = 0;
+    unsigned masks[kSplitItems];
+#pragma unroll
+    for (int k = 0; k < kSplitItems; ++k) {
+        const int i = wbase + k * 32 + lane;
+        const bool f = i < n && V.split_flag[i] != 0;
+        masks[k] = __ballot_sync(0xffffffffu, f);
+        warp_count += __popc(masks[k]);
+    }
+    if (lane == 0) s_warp[warp] = warp_count;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < kSplitThreads / 32 ? s_warp[lane] : 0u;
+        unsigned wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < kSplitThreads / 32) s_warp[lane] = wi - w;
+        const unsigned total = __shfl_sync(0xffffffffu, wi, kSplitThreads / 32 - 1);
+        const unsigned prefix = lookback_prefix(V.split_tiles, tile, total, &V.cnt->err);
+        if (lane == 0) {
+            s_prefix = prefix;
+            if (tile == ntiles - 1) {
+                const int nsplit = static_cast<int>(prefix + total);
+                long long want = static_cast<long long>(nH) + 4LL * nsplit;
+                V.cnt->n_split = nsplit;
+                if (want > P.capH) {
+                    atomicOr(&V.cnt->err, kErrCapacity);
+                    want = nH + 4LL * ((P.capH - nH) / 4);
+                }
+                V.cnt->next[1] = static_cast<int>(want);
+                V.cnt->next[0] = n;
+            }
+        }
+    }
+    __syncthreads();
+    unsigned rank = s_prefix + s_warp[warp];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll 1
+    for (int k = 0; k < kSplitItems; ++k) {
+        const unsigned m = masks[k];
+        if (m & (1u << lane)) {
+            const int i = wbase + k * 32 + lane;
+            const unsigned r = rank + __popc(m & lt);
+            if (r >= static_cast<unsigned>(n)) {  // only after a failed look-back
+                atomicOr(&V.cnt->err, kErrTimeout);
+                rank += __popc(m);
+                continue;
+            }
+            const int id = V.L.id[i];
+            V.split_ids[r] = id;
+            const long long hb = static_cast<long long>(nH) + 4LL * r;
+            if (hb + 4 <= P.capH) {
+                const float2 p = V.L.npos[i], v = V.L.nvel[i];
+                const float rho = V.L.dens[i];
+                const float rad = static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) /
+                                                                 (static_cast<double>(2.0f * rho) * kPi)));
+                const float2 cp[4] = {make_float2(p.x + rad, p.y + rad), make_float2(p.x - rad, p.y + rad),
+                                      make_float2(p.x + rad, p.y - rad), make_float2(p.x - rad, p.y - rad)};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int h = static_cast<int>(hb) + c;
+                    V.H.npos[h] = cp[c];
+                    V.H.nvel[h] = v;
+                    V.H.nst[h] = 1;
+                    V.H.nid[h] = 4 * id + c;
+                    if (V.H.ndens) {
+                        V.H.ndens[h] = 0.0f;
+                        V.H.npres[h] = 0.0f;
+                    }
+                }
+            }
+        }
+        rank += __popc(m);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// High-res force + integrate + tether: computeParticleAccelerationAndAdvanceHigh
+// (WCSPHSolver.cu:1867-2033) and adjustOrInjectTransientHighD (1097-1172).
+// Reads see the pre-step state (the reference integrates in place, a data race);
+// low-res states are read after this step's split marks, as in the reference.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_force_high(Params P, StepView V) {
+    const int n = V.cnt->cur[1];
+    const ScaleView& H = V.H;
+    const ScaleView& L = V.L;
+    for (int i = tid(); i < n; i += nthreads()) {
+        float2 p = H.pos[i], v = H.vel[i];
+        const unsigned s = H.st[i];
+        const float dens = H.dens[i], qi = H.q[i];
+        float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f);
+        float2 accT = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
+        int csx, csy, cex, cey;
+        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimH[0];
+            const int b = H.off[row + cex + 1];
+            for (int j = H.off[row + csx]; j < b; ++j) {
+                if (!lamHH(s, H.st[j])) continue;
+                const float2 pij = sub(p, H.pos[j]);
+                const float dist = vnorm(pij);
+                if (dist != 0.0f && dist < P.rh)
+                    pair_force(P, pij, dist, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
+            }
+        }
+        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = L.off[row + cex + 1];
+            for (int j = L.off[row + csx]; j < b; ++j) {
+                const unsigned sj = L.nst[j];
+                if (!(lamHL(s, sj) && notDeleted(sj))) continue;
+                const float2 pij = sub(p, L.pos[j]);
+                const float dist = vnorm(pij);
+                if (dist != 0.0f && dist < P.r)
+                    pair_force(P, pij, dist, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
+            }
+            const int wb = V.woff[row + cex + 1];
+            for (int k = V.woff[row + csx]; k < wb; ++k) {
+                const float2 pik = sub(p, V.wpos[k]);
+                const float gm = wall_weight(vnorm(pik), P.rh, P.cs);
+                accB.x += P.cBH * gm * pik.x;
+                accB.y += P.cBH * gm * pik.y;
+            }
+        }
+        acc.x *= -P.mH;
+        acc.y *= -P.mH;
+        accL.x *= -P.mL;
+        accL.y *= -P.mL;
+        acc.x -= P.sigma * accT.x;
+        acc.y -= P.sigma * accT.y;
+        acc.x += accL.x;
+        acc.y += accL.y;
+        acc.x += accB.x;
+        acc.y += accB.y;
+        acc.y -= P.g;
+        H.acc[i] = acc;
+        if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+        v.x += P.dt * acc.x;
+        v.y += P.dt * acc.y;
+        p.x += P.dt * v.x;
+        p.y += P.dt * v.y;
+        // tether to the parent after the parent's advance (adjustPosition, 1007-1022)
+        const int id = H.id[i];
+        const int parent = id >> 2;
+        if (parent >= 0 && parent < P.slotsL) {
+            const int pi = L.map[parent];
+            if (pi >= 0 && L.st[pi] == 1) {
+                const float2 pl = L.npos[pi];
+                const float rho = L.dens[pi];
+                const float2 pji = sub(p, pl);
+                const float dist = vnorm(pji);
+                const float lim = static_cast<float>(
+                    fmin(static_cast<double>(dist),
+                         0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(rho) * kPi))));
+                p.x = pl.x + lim / dist * pji.x;
+                p.y = pl.y + lim / dist * pji.y;
+            }
+        }
+        H.npos[i] = p;
+        H.nvel[i] = v;
+        H.nst[i] = static_cast<uint8_t>(s);
+        H.nid[i] = id;
+        if (H.ndens) {
+            H.ndens[i] = dens;
+            H.npres[i] = H.pres[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Relaxation of the children created in the previous step (older snapshot,
+// TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:2380-2446): density 1133-1217,
+// pressure + wall force 1499-1622 (= TwoScale2D/WCSPHSolver.cu:2035-2158), dt/10.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_relax_density(Params P, StepView V) {
+    const int nf = min(4 * V.cnt->n_fresh, P.capH);  // relaxation scratch holds capH entries
+    const ScaleView& H = V.H;
+    const ScaleView& L = V.L;
+    for (int f = tid(); f < nf; f += nthreads()) {
+        const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
+        const int i = (slot >= 0 && slot < P.slotsH) ? H.map[slot] : -1;
+        if (i < 0) continue;
+        const float2 p = H.pos[i];
+        float d = 0.0f, dl = 0.0f;
+        int csx, csy, cex, cey;
+        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimH[0];
+            const int b = H.off[row + cex + 1];
+            for (int j = H.off[row + csx]; j < b; ++j) {
+                float dist = vnorm(sub(p, H.pos[j]));
+                if (dist <= P.rh) d += kernW(dist, P.rh, P.CH);
+            }
+        }
+        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = L.off[row + cex + 1];
+            for (int j = L.off[row + csx]; j < b; ++j) {
+                float dist = vnorm(sub(p, L.pos[j]));
+                if (dist <= P.rh) dl += kernW(dist, P.rh, P.CH);
+            }
+        }
+        d *= P.mH;
+        dl *= P.mL;
+        d += dl;
+        H.dens[i] = d;
+        H.pres[i] = tait(d, P);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_relax_force(Params P, StepView V) {
+    const int nf = min(4 * V.cnt->n_fresh, P.capH);  // relaxation scratch holds capH entries
+    const ScaleView& H = V.H;
+    const ScaleView& L = V.L;
+    for (int f = tid(); f < nf; f += nthreads()) {
+        const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
+        const int i = (slot >= 0 && slot < P.slotsH) ? H.map[slot] : -1;
+        if (i < 0) continue;
+        float2 p = H.pos[i], v = H.vel[i];
+        const float dens = H.dens[i], pre = H.pres[i];
+        const float dens2 = dens * dens;
+        float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
+        int csx, csy, cex, cey;
+        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimH[0];
+            const int b = H.off[row + cex + 1];
+            for (int j = H.off[row + csx]; j < b; ++j) {
+                const float2 pij = sub(p, H.pos[j]);
+                const float dist = vnorm(pij);
+                if (dist != 0.0f && dist < P.rh) {
+                    const float dj = H.dens[j];
+                    const float coeff = pre / dens2 + H.pres[j] / (dj * dj);
+                    const float2 g = kernDW(pij, dist, P.rh, P.GH);
+                    acc.x += coeff * g.x;
+                    acc.y += coeff * g.y;
+                }
+            }
+        }
+        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = L.off[row + cex + 1];
+            for (int j = L.off[row + csx]; j < b; ++j) {
+                const float2 pij = sub(p, L.pos[j]);
+                const float dist = vnorm(pij);
+                if (dist != 0.0f && dist < P.rh) {
+                    const float dj = L.dens[j];
+                    const float coeff = pre / dens2 + L.pres[j] / (dj * dj);
+                    const float2 g = kernDW(pij, dist, P.rh, P.GH);
+                    accL.x += coeff * g.x;
+                    accL.y += coeff * g.y;
+                }
+            }
+            const int wb = V.woff[row + cex + 1];
+            for (int k = V.woff[row + csx]; k < wb; ++k) {
+                const float2 pik = sub(p, V.wpos[k]);
+                const float gm = wall_weight(vnorm(pik), P.rh, P.cs);
+                accB.x += P.cBH * gm * pik.x;
+                accB.y += P.cBH * gm * pik.y;
+            }
+        }
+        acc.x *= -P.mH;
+        acc.y *= -P.mH;
+        accL.x *= -P.mL;
+        accL.y *= -P.mL;
+        acc.x += accL.x;
+        acc.y += accL.y;
+        acc.x += accB.x;
+        acc.y += accB.y;
+        v.x += P.relax_dt * acc.x;
+        v.y += P.relax_dt * acc.y;
+        p.x += P.relax_dt * v.x;
+        p.y += P.relax_dt * v.y;
+        V.relax_pos[f] = p;
+        V.relax_vel[f] = v;
+    }
+}
+
+__global__ void k_relax_apply(Params P, StepView V) {
+    const int nf = min(4 * V.cnt->n_fresh, P.capH);  // relaxation scratch holds capH entries
+    for (int f = tid(); f < nf; f += nthreads()) {
+        const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
+        const int i = (slot >= 0 && slot < P.slotsH) ? V.H.map[slot] : -1;
+        if (i < 0) continue;
+        const_cast<float2*>(V.H.pos)[i] = V.relax_pos[f];
+        const_cast<float2*>(V.H.vel)[i] = V.relax_vel[f];
+    }
+}
+
+__global__ void k_step_finish(Counters* c) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        c->sorted[0] = c->cur[0];
+        c->sorted[1] = c->cur[1];
+        c->cur[0] = c->next[0];
+        c->cur[1] = c->next[1];
+        c->n_fresh = c->n_split;
+        c->h_state0 = 0;
+        c->steps += 1;
+        for (int k = 0; k < 8; ++k) c->tile_ctr[k] = 0;
+    }
+}
+
+}  // namespace tss

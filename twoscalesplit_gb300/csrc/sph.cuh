@@ -1,0 +1,56 @@
+// sph.cuh -- the gather kernels of one two-scale WCSPH step.
+#pragma once
+#include "tss_device.cuh"
+
+namespace tss {
+
+// One scale's arrays.  "cur" arrays are in this step's (cell, id) order, "list"
+// arrays (n*) hold the state the next step starts from, in that same order for
+// existing particles, with newly created high-res children appended.
+struct ScaleView {
+    const float2* pos;
+    const float2* vel;
+    const uint8_t* st;
+    const int32_t* id;
+    float* dens;
+    float* pres;
+    float* q;        // p / rho^2
+    float2* acc;
+    const int* off;  // dense cell offsets [C+1]
+    int32_t* map;    // slot id -> index in the cur arrays
+    float2* npos;
+    float2* nvel;
+    uint8_t* nst;
+    int32_t* nid;
+    float* ndens;    // carried densities/pressures (relaxation only; may be null)
+    float* npres;
+};
+
+struct StepView {
+    ScaleView L, H;
+    const float2* wpos;     // walls in (low cell, id) order
+    const int* woff;        // wall cell offsets on the low grid
+    Counters* cnt;
+    uint8_t* split_flag;    // [n_low]
+    int32_t* split_ids;     // [n_low] parents split this step (= next step's fresh list)
+    unsigned long long* split_tiles;
+    float2* relax_pos;      // [capH] relaxation scratch
+    float2* relax_vel;
+    int nL;                 // low-res count (constant for a solver)
+};
+
+constexpr int kSplitThreads = 256;
+constexpr int kSplitItems = 16;
+constexpr int kSplitTile = kSplitThreads * kSplitItems;
+
+__global__ void k_density_high(Params P, StepView V);
+__global__ void k_density_low(Params P, StepView V);
+__global__ void k_force_low(Params P, StepView V);
+__global__ void k_split(Params P, StepView V);
+__global__ void k_force_high(Params P, StepView V);
+__global__ void k_relax_density(Params P, StepView V);
+__global__ void k_relax_force(Params P, StepView V);
+__global__ void k_relax_apply(Params P, StepView V);
+__global__ void k_step_finish(Counters* c);
+
+}  // namespace tss

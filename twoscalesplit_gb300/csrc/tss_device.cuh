@@ -1,0 +1,202 @@
+// tss_device.cuh -- device-side types and per-pair arithmetic of the two-scale
+// WCSPH step.  Every expression keeps the reference's FP32 operation order
+// (TwoScale2D/WCSPHSolver.cu:66-333, 476-954) and the library is compiled with
+// --fmad=false and IEEE division/square root, so a kernel's result is the
+// reference's result for the same summation order, bit for bit.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tss {
+
+constexpr double kPi = 3.14159265358979323846;  // WCSPHSolver.cu:19
+
+// error word bits (mirror TSS_ERR_* in include/tss.h)
+constexpr unsigned kErrCapacity = 0x1u;
+constexpr unsigned kErrNumeric = 0x2u;
+constexpr unsigned kErrTimeout = 0x4u;
+
+// Spin limit for decoupled look-back waits; ~0.5 s with the back-off below.
+constexpr int kSpinLimit = 1 << 22;
+
+struct Params {
+    float ox, oy;
+    int dimL[2], dimH[2];
+    float r, rh, rho0, B, cs, alpha, sigma, dt, g;
+    float CL, GL, CH, GH;  // kernel / gradient coefficients (Bind, WCSPHSolver.cu:2559-2590)
+    float mL, mH, mB;
+    float cBL, cBH;        // mB/(mL+mB), mB/(mH+mB)
+    float hx;              // (r + rh) / 2, the cross-scale viscosity length
+    float relax_dt;
+    float roi[4];
+    int relax_iters;
+    int q1;
+    int slotsL, slotsH;    // slot-id spaces: low ids < slotsL, high ids < slotsH = 4*slotsL
+    int capH;
+};
+
+// Device-side counters of one solver.  `cur` is what this step's kernels use;
+// `next` is what the step produces; the step's last kernel copies next -> cur.
+struct Counters {
+    int cur[2];
+    int next[2];
+    int n_fresh;     // parents split in the previous step (relaxed this step)
+    int n_split;     // parents split in this step
+    unsigned err;    // kErr* bits
+    int h_state0;    // 1 if some high-res particle has (state & 1) == 0
+    long long steps;
+    int sorted[2];   // particles sorted in the last step (its `cur` counts)
+    int tile_ctr[8]; // tile claim counters for the look-back passes of one step
+};
+
+__device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating
+
+// computeGridCoordinate(pos, offset), WCSPHSolver.cu:265-289
+__device__ __forceinline__ void grid_coord(float px, float py, float off, float ox, float oy, float cell,
+                                           int dimx, int dimy, int& cx, int& cy) {
+    cx = f2i(((px + off) - ox) / cell);
+    cy = f2i(((py + off) - oy) / cell);
+    cx = min(max(0, cx), dimx - 1);
+    cy = min(max(0, cy), dimy - 1);
+}
+
+__device__ __forceinline__ int cell_hash(float2 p, float ox, float oy, float cell, int dimx, int dimy) {
+    int cx, cy;
+    grid_coord(p.x, p.y, 0.0f, ox, oy, cell, dimx, dimy, cx, cy);
+    return cy * dimx + cx;
+}
+
+// evaluateM4Kernel(High), WCSPHSolver.cu:116-160
+__device__ __forceinline__ float kernW(float d, float rad, float C) {
+    float q = d * 2.0f / rad;
+    if (q < 1.0f) {
+        float a = 2.0f - q, b = 1.0f - q;
+        return C * (a * a * a - 4.0f * b * b * b);
+    } else if (q < 2.0f) {
+        float a = 2.0f - q;
+        return C * a * a * a;
+    }
+    return 0.0f;
+}
+
+// evaluateGradientM4Kernel(High), WCSPHSolver.cu:162-239
+__device__ __forceinline__ float2 kernDW(float2 x, float d, float rad, float G) {
+    float q = d * 2.0f / rad;
+    if (q < 1.0f) {
+        float a = 2.0f - q, b = 1.0f - q;
+        float c = G * (a * a - 4.0f * b * b) / d;
+        return make_float2(c * x.x, c * x.y);
+    } else if (q < 2.0f) {
+        float a = 2.0f - q;
+        float c = G * a * a / d;
+        return make_float2(c * x.x, c * x.y);
+    }
+    return make_float2(0.0f, 0.0f);
+}
+
+// evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114
+__device__ __forceinline__ float wall_weight(float d, float rad, float cs) {
+    float q = d * 2.0f / rad;
+    float c = 0.02f * cs * cs / (d * d);
+    if (q < 2.0f / 3.0f) return c * 2.0f / 3.0f;
+    if (q < 1.0f) return c * (2.0f * q - 3.0f / 2.0f * q * q);
+    if (q < 2.0f) {
+        float a = 2.0f - q;
+        return c * 0.5f * a * a;
+    }
+    return 0.0f;
+}
+
+__device__ __forceinline__ float vnorm(float2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
+
+__device__ __forceinline__ float tait(float dens, const Params& P) {
+    float a = dens / P.rho0;
+    float a3 = a * a * a;
+    return P.B * (a3 * a3 * a - 1.0f);
+}
+
+// lambda masks indexed by (s_i & 1) << 1 | (s_j & 1); all entries are 0 or 1, so
+// they act as predicates (a weight of 1 leaves every product unchanged).
+__device__ __forceinline__ bool lamLH(unsigned si, unsigned sj) { return (sj & 1u) == 0u; }        // {1,0,1,0}
+__device__ __forceinline__ bool lamHH(unsigned si, unsigned sj) { return !((si & 1u) == 0u && (sj & 1u)); }  // {1,0,1,1}
+__device__ __forceinline__ bool lamHL(unsigned si, unsigned sj) { return !((si & 1u) && (sj & 1u)); }        // {1,1,1,0}
+__device__ __forceinline__ bool notDeleted(unsigned s) { return s < 2u; }                       // {1,1,0}
+
+// One pair of a force sum: the body of updateAccCell / updateAccCellComplement /
+// updateAccCellHigh / updateAccCellComplementHigh (WCSPHSolver.cu:521-558 etc.).
+// qi, qj are p/rho^2 of the two particles (the reference's pre/dens2, prej/densj2).
+__device__ __forceinline__ void pair_force(const Params& P, float2 pij, float dist, float2 vij, float qi, float qj,
+                                           float densi, float densj, float h, float2& acc, float2& accT) {
+    float coeff = qi + qj;
+    float dvp = vij.x * pij.x + vij.y * pij.y;
+    if (dvp < 0.0f) coeff -= dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
+    float2 gI = kernDW(pij, dist, P.r, P.GL);
+    float2 gJ = kernDW(pij, dist, P.rh, P.GH);
+    acc.x += coeff * (gI.x + gJ.x) / 2.0f;
+    acc.y += coeff * (gI.y + gJ.y) / 2.0f;
+    float w = kernW(dist, P.r, P.CL);
+    float w2 = kernW(dist, P.rh, P.CH);
+    accT.x += pij.x * (w + w2) / 2.0f;
+    accT.y += pij.y * (w + w2) / 2.0f;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Decoupled look-back (single-pass prefix over tiles).  Called by all 32 lanes of
+// warp 0 of the block owning `tile`; publishes the tile's aggregate, walks back
+// over predecessors 32 at a time, publishes the inclusive prefix and returns the
+// exclusive prefix (in every lane).  Status word: flag << 32 | value, flag 1 =
+// aggregate only, 2 = inclusive prefix.  Waits are bounded: after kSpinLimit polls
+// the error word gets kErrTimeout and the tile proceeds with what it has.
+__device__ __forceinline__ unsigned lookback_prefix(unsigned long long* state, int tile, unsigned aggregate,
+                                                    unsigned* err) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) st_release_u64(&state[0], (2ull << 32) | aggregate);
+        return 0u;
+    }
+    if (lane == 0) st_release_u64(&state[tile], (1ull << 32) | aggregate);
+    unsigned prefix = 0;
+    int window = tile - 1;
+    while (true) {
+        int t = window - lane;
+        unsigned long long w = 2ull << 32;  // before tile 0: an inclusive zero
+        if (t >= 0) {
+            int spins = 0;
+            while (true) {
+                w = ld_acquire_u64(&state[t]);
+                if ((w >> 32) != 0) break;
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, kErrTimeout);
+                    w = 2ull << 32;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        unsigned flag = unsigned(w >> 32);
+        unsigned val = unsigned(w);
+        unsigned inc_mask = __ballot_sync(0xffffffffu, flag == 2u);
+        if (inc_mask) {
+            int stop = __ffs(inc_mask) - 1;  // closest predecessor with an inclusive prefix
+            unsigned contrib = lane <= stop ? val : 0u;
+            for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+            prefix += contrib;
+            break;
+        }
+        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+        prefix += val;
+        window -= 32;
+    }
+    if (lane == 0) st_release_u64(&state[tile], (2ull << 32) | (prefix + aggregate));
+    return prefix;
+}
+
+}  // namespace tss

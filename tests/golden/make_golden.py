@@ -68,7 +68,7 @@ def _ref_state(ref, scale):
 
 
 def step_case(fname, relax_iters, warm_steps):
-    sc = scenes.dam_break_small(20, 40, seed=7, relax_iters=relax_iters)
+    sc = scenes.dam_break_small(20, 40, seed=7, relax_iters=relax_iters, calibrate_mass=False)
     sc.config.roi[:] = REF_ROI
     ref = O.RefCPU(sc)
     for _ in range(warm_steps):

@@ -90,7 +90,8 @@ def test_step_matches_reference_fixture_bit_exact(fname):
 @pytest.mark.skipif(not O.refcpu_available(), reason="needs the reference checkout")
 @pytest.mark.parametrize("relax", [0, 4])
 def test_oracle_tracks_reference_kernels_many_steps(relax):
-    sc = scenes.dam_break_small(16, 32, seed=11, relax_iters=relax)
+    # the literal mass (1000 dx^2) starts violently, so splits at x > 0.5 come early
+    sc = scenes.dam_break_small(16, 32, seed=11, relax_iters=relax, calibrate_mass=False)
     sc.config.roi[:] = REF_ROI
     orc = O.Oracle(sc, 32)
     ref = O.RefCPU(sc)
@@ -167,9 +168,11 @@ def test_lattice_density_and_tait():
     d = np.linalg.norm(p - p[15 * 30 + 15], axis=1)
     w = [0.5 * (O.kernel_eval(0, x, r) + O.kernel_eval(0, x, rh)) for x in d[d <= r]]
     assert dens[i] == pytest.approx(m * sum(w), rel=1e-12)
-    # the low-res kernel alone reproduces the rest density on a perfect lattice
+    # the generator's mass calibration puts the lattice at rest density ...
+    assert dens[i] == pytest.approx(1000.0, rel=1e-4)
+    # ... while the low-res kernel alone with mass rho0 dx^2 also sums to rho0
     w_r = sum(O.kernel_eval(0, x, r) for x in d[d <= r])
-    assert m * w_r == pytest.approx(1000.0, rel=0.01)
+    assert 1000.0 * dx * dx * w_r == pytest.approx(1000.0, rel=0.01)
     # Tait: p = B((rho/rho0)^7 - 1)
     B = sc.config.tait_b
     assert pres[i] == pytest.approx(B * ((dens[i] / 1000.0) ** 7 - 1), rel=1e-9)

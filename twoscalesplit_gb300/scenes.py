@@ -18,6 +18,19 @@ layers of fixed particles around [0,1]^2 at half the fluid spacing; the grid
 domain is padded by 4 wall spacings so that the walls lie inside it.  Every
 lattice coordinate is jittered by U(+-1e-4 * spacing) from the seed.
 dt for dam_break_1m keeps the Courant number of dam_break_5k: dt = 1e-4 * dx/0.008.
+
+Two choices keep these scenes physical (both are switches):
+  * mass: with support 2 x spacing the pair kernel (W_r + W_rh)/2 sums to 1.41/dx^2
+    on the lattice, so mass 1000*dx^2 starts the fluid at 1.41 rho0, i.e. at a
+    pressure of ~10 B, and the block explodes through its walls within ~100
+    steps.  `calibrate_mass` (default on) scales the mass by rho0 / (lattice
+    density), 0.709, so the lattice starts at rest density.
+  * relaxation: the older snapshot's relaxation (4 x dt/10 with the single-scale
+    high-res kernel) applied to children placed as the current tree places them
+    (0.5*sqrt(m/(2 rho pi)) from the parent) gives them 2-3 rho0 in the first
+    sub-step and throws them apart.  The workloads run with relax_iters = 0, as
+    the current reference tree does (its relaxTransient call is commented out,
+    WCSPHSolver.cu:2738); relax_iters=4 selects the relaxation.
 """
 import dataclasses
 import math
@@ -86,7 +99,22 @@ def particle_box_canvas(xs, ys, dx, dim_x, dim_y, off_x, off_y):
     return np.concatenate(out, axis=0)
 
 
-def _dam_break(name, nx, ny, dx, roi, dt, steps, cap_high, relax_iters, seed, flags=None):
+def lattice_pair_kernel_sum(dx, r, rh):
+    """sum_j (W_r + W_rh)(|x_ij|) / 2 over an infinite square lattice of spacing dx."""
+    k = int(math.ceil(r / dx)) + 1
+    a = np.arange(-k, k + 1, dtype=np.float64)
+    d = np.hypot(*np.meshgrid(a * dx, a * dx)).ravel()
+    d = d[d <= r]
+
+    def w(d, s):
+        q = 2.0 * d / s
+        c = 20.0 / (14.0 * math.pi * s * s)
+        return np.where(q < 1, c * ((2 - q) ** 3 - 4 * (1 - q) ** 3), np.where(q < 2, c * (2 - q) ** 3, 0.0))
+
+    return float(np.sum(0.5 * (w(d, r) + w(d, rh))))
+
+
+def _dam_break(name, nx, ny, dx, roi, dt, steps, cap_high, relax_iters, seed, flags=None, calibrate_mass=True):
     rng = np.random.default_rng(seed)
     dx = float(np.float32(dx))
     low = particle_box(0.5 * dx, 0.5 * dx, dx, nx, ny)
@@ -104,20 +132,22 @@ def _dam_break(name, nx, ny, dx, roi, dt, steps, cap_high, relax_iters, seed, fl
     if flags is not None:
         cfg.flags = flags
     m = REST_DENSITY * dx * dx
+    if calibrate_mass:
+        m = REST_DENSITY / lattice_pair_kernel_sum(dx, float(cfg.r_low), float(cfg.r_high))
     return Scene(name=name, config=cfg, low_pos=low, low_vel=np.zeros_like(low), mass_low=m,
                  mass_high=m / 4.0, cap_high=cap_high, wall_pos=walls,
                  mass_wall=REST_DENSITY * wdx * wdx, steps=steps, dx=dx)
 
 
-def dam_break_5k(seed=0, **kw):
+def dam_break_5k(seed=0, relax_iters=0, **kw):
     return _dam_break("dam_break_5k", 50, 100, 0.008, [0.4, 0.0, 0.7, 0.3], 1e-4, 2000,
-                      4 * 5000, 4, seed, **kw)
+                      4 * 5000, relax_iters, seed, **kw)
 
 
-def dam_break_1m(seed=0, **kw):
+def dam_break_1m(seed=0, relax_iters=0, **kw):
     dx = 5.66e-4
     return _dam_break("dam_break_1m", 707, 1414, dx, [0.4, 0.0, 0.9, 0.5], 1e-4 * dx / 0.008, 500,
-                      4_000_000, 4, seed, **kw)
+                      4_000_000, relax_iters, seed, **kw)
 
 
 def dam_break_small(nx, ny, dx=None, seed=0, roi=None, relax_iters=4, cap_high=None, **kw):

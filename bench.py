@@ -88,7 +88,8 @@ class ClockSampler:
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+            sel = [f"--id={self.gpu}"] if self.gpu not in (None, "") else []
+            self.proc = subprocess.Popen(["nvidia-smi", *sel, f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -215,7 +216,8 @@ def run_ours(args):
     reset()
     K = args.steps
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    clocks = ClockSampler(local if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+    clocks = ClockSampler(vis[local].strip() if local < len(vis) and vis[local].strip() else (str(local) if world > 1 else None))
     clocks.start()
     time.sleep(0.3)
     if world > 1:

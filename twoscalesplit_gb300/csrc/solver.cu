@@ -152,7 +152,11 @@ struct tss_solver {
     }
 
     // Enqueue one step (the body of AdvanceTS, WCSPHSolver.cu:2726-2810).
-    cudaError_t mark(int k, cudaStream_t s) { return profile ? cudaEventRecord(ev[k], s) : cudaSuccess; }
+    // cudaEventRecordExternal makes the record a node of the captured graph (a plain
+    // record inside capture only orders streams)
+    cudaError_t mark(int k, cudaStream_t s) {
+        return profile ? cudaEventRecordWithFlags(ev[k], s, cudaEventRecordExternal) : cudaSuccess;
+    }
 
     cudaError_t enqueue_step(cudaStream_t s) {
         cudaError_t e;

@@ -198,7 +198,10 @@ def run_ours(args):
     build.build()
     sc = scenes.make_scene(args.scene, seed=rank)
     sol = Solver.from_scene(sc)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the graph replays, the L2 flush and the timing events all
+    # go to it, so the events bracket exactly the step
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
     init_low = sol.download(0)
     empty = {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32), "vel": np.zeros((0, 2), np.float32),

@@ -96,9 +96,10 @@ tss_status tss_solver_create(const tss_config* cfg,
 void tss_solver_destroy(tss_solver* s);
 
 /* Advance n_steps steps (WCSPHSolver::AdvanceTS, WCSPHSolver.cu:2726-2810), enqueued
- * on `stream` (a cudaStream_t; NULL = the solver's own stream).  Nothing is copied
- * back to the host; the particle counts stay on the device.  The first call
- * captures the step into a CUDA graph; later calls replay it. */
+ * on `stream` (a cudaStream_t; NULL = the default stream, as the reference used).
+ * Nothing is copied back to the host; the particle counts stay on the device.  The
+ * first call captures the step into a CUDA graph (on a private stream); later calls
+ * replay it. */
 tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream);
 
 /* Block until all enqueued work is done; returns the device error word mapped to a

@@ -23,27 +23,46 @@ int particle_blocks(int cap, int threads) {
 
 __global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restrict__ n_ptr, float ox, float oy,
                             float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
-                            int* __restrict__ rank) {
+                            int* __restrict__ rank, unsigned* __restrict__ tile_sum) {
     const int n = *n_ptr;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int c = cell_hash(pos[i], ox, oy, cell, dimx, dimy);
-        key[i] = c;
-        rank[i] = static_cast<int>(atomicAdd(&count[c], 1u));
+    const int lane = threadIdx.x & 31;
+    // warp-uniform trip count, so the ballot/match below see whole warps
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool act = i < n;
+        int c = 0;
+        if (act) {
+            c = cell_hash(pos[i], ox, oy, cell, dimx, dimy);
+            key[i] = c;
+            rank[i] = static_cast<int>(atomicAdd(&count[c], 1u));
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, act);
+        if (act) {
+            const unsigned t = static_cast<unsigned>(c) / kScanTile;
+            const unsigned peers = __match_any_sync(mask, t);
+            if (lane == __ffs(peers) - 1) atomicAdd(&tile_sum[t], static_cast<unsigned>(__popc(peers)));
+        }
     }
 }
 
-// One tile of kScanTile counts per block, tiles claimed in launch order.
-__global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g, int* tile_ctr, unsigned* err) {
-    __shared__ int s_tile;
+// One tile of kScanTile counts per block.  The tile's offset is the sum of the
+// tile sums before it (at most a few thousand, read from L2), so tiles are
+// independent and nothing waits on another block.
+__global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
     __shared__ unsigned s_warp[kScanThreads / 32];
-    __shared__ unsigned s_prefix;
-    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1);
-    __syncthreads();
-    const int tile = s_tile;
+    __shared__ unsigned s_red[kScanThreads / 32];
+    const int tile = blockIdx.x;
     const int C = g.ncells;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned before = 0;
+    for (int t = threadIdx.x; t < tile; t += blockDim.x) before += g.tile_sum[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) s_red[warp] = before;
     const int base = tile * kScanTile + threadIdx.x * kScanItems;
     unsigned v[kScanItems];
-    if (base + kScanItems <= C) {
+    const bool full = base + kScanItems <= C;
+    if (full) {
         const uint4* p = reinterpret_cast<const uint4*>(g.count + base);
         uint4 a = p[0], b = p[1];
         v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
@@ -62,8 +81,6 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g, int* til
     unsigned sum = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) sum += v[k];
-    // block-wide exclusive scan of the per-thread sums
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned inc = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -74,27 +91,38 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g, int* til
     __syncthreads();
     if (warp == 0) {
         unsigned w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+        unsigned r = lane < kScanThreads / 32 ? s_red[lane] : 0u;
         unsigned wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
             if (lane >= o) wi += t;
         }
-        if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-        unsigned total = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
-        unsigned prefix = lookback_prefix(g.tile_state, tile, total, err);
-        if (lane == 0) s_prefix = prefix;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (lane < kScanThreads / 32) s_warp[lane] = wi - w + r;  // exclusive warp offsets + tile prefix
     }
     __syncthreads();
-    unsigned run = s_prefix + s_warp[warp] + (inc - sum);
+    unsigned run = s_warp[warp] + (inc - sum);
+    unsigned o8[kScanItems];
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-        int idx = base + k;
-        if (idx < C) g.off[idx] = static_cast<int>(run);
+        o8[k] = run;
         run += v[k];
-        if (idx == C - 1) g.off[C] = static_cast<int>(run);
     }
-    if (C == 0 && tile == 0 && threadIdx.x == 0) g.off[0] = 0;
+    if (full) {
+        int4* q = reinterpret_cast<int4*>(g.off + base);
+        q[0] = make_int4(o8[0], o8[1], o8[2], o8[3]);
+        q[1] = make_int4(o8[4], o8[5], o8[6], o8[7]);
+        if (base + kScanItems == C) g.off[C] = static_cast<int>(run);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            int idx = base + k;
+            if (idx < C) g.off[idx] = static_cast<int>(o8[k]);
+            if (idx == C - 1) g.off[C] = static_cast<int>(o8[k] + v[k]);
+        }
+    }
 }
 
 // Every index below is checked: if a look-back wait gave up (kErrTimeout) the
@@ -156,8 +184,7 @@ size_t grid_bufs_bytes(int cap, int ncells) {
     int ntiles = (ncells + kScanTile - 1) / kScanTile;
     if (ntiles < 1) ntiles = 1;
     return al(sizeof(unsigned) * (size_t)ncells) + al(sizeof(int) * ((size_t)ncells + 1)) +
-           al(sizeof(int) * (size_t)cap) * 2 + al(sizeof(int2) * (size_t)cap) +
-           al(sizeof(unsigned long long) * (size_t)ntiles);
+           al(sizeof(int) * (size_t)cap) * 2 + al(sizeof(int2) * (size_t)cap) + al(sizeof(unsigned) * (size_t)ntiles);
 }
 
 GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
@@ -177,20 +204,19 @@ GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
     p += al(sizeof(int) * (size_t)cap);
     g.perm = reinterpret_cast<int2*>(p);
     p += al(sizeof(int2) * (size_t)cap);
-    g.tile_state = reinterpret_cast<unsigned long long*>(p);
+    g.tile_sum = reinterpret_cast<unsigned*>(p);
     return g;
 }
 
 cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
-                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, int* tile_ctr,
-                               unsigned* err, cudaStream_t stream) {
+                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
+                               cudaStream_t stream) {
     const int T = 256;
     const int pb = particle_blocks(cap, T);
     cudaError_t e;
-    if ((e = cudaMemsetAsync(g.tile_state, 0, sizeof(unsigned long long) * g.ntiles, stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(tile_ctr, 0, sizeof(int), stream)) != cudaSuccess) return e;
-    k_grid_keys<<<pb, T, 0, stream>>>(pos, n_ptr, ox, oy, cell, dimx, dimy, g.count, g.key, g.rank);
-    k_grid_scan<<<g.ntiles, kScanThreads, 0, stream>>>(g, tile_ctr, err);
+    if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
+    k_grid_keys<<<pb, T, 0, stream>>>(pos, n_ptr, ox, oy, cell, dimx, dimy, g.count, g.key, g.rank, g.tile_sum);
+    k_grid_scan<<<g.ntiles, kScanThreads, 0, stream>>>(g);
     k_grid_scatter<<<pb, T, 0, stream>>>(n_ptr, id, g, err);
     k_grid_reorder<<<pb, T, 0, stream>>>(n_ptr, g, a, err);
     return cudaGetLastError();
@@ -204,7 +230,7 @@ __global__ void k_set_int(int* p, int v) { *p = v; }
 // C ABI: grid build on caller-owned device memory
 // ---------------------------------------------------------------------------
 namespace {
-// workspace layout: [n + tile counter + error word (256 B)] [grid buffers] [scratch pos copy]
+// workspace layout: [n + error word (256 B)] [grid buffers] [scratch pos copy]
 size_t ws_bytes(int n, int dimx, int dimy) {
     size_t cells = static_cast<size_t>(dimx) * static_cast<size_t>(dimy);
     int cap = n > 0 ? n : 1;
@@ -231,7 +257,6 @@ extern "C" tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, in
     const int cap = n > 0 ? n : 1;
     char* w = static_cast<char*>(d_workspace);
     int* n_dev = reinterpret_cast<int*>(w);
-    int* tile_ctr = n_dev + 1;
     unsigned* err = reinterpret_cast<unsigned*>(n_dev + 2);
     tss::GridBufs g = tss::grid_bufs_carve(w + 256, cap, cells);
     g.off = d_cell_off;  // write the offsets straight into the caller's table
@@ -244,6 +269,6 @@ extern "C" tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, in
     a.dst_pos = scratch;
     a.dst_order = d_order;
     cudaError_t e = tss::grid_build_enqueue(reinterpret_cast<const float2*>(d_pos), d_id, n_dev, cap, origin_x, origin_y,
-                                            cell_size, dimx, dimy, g, a, tile_ctr, err, st);
+                                            cell_size, dimx, dimy, g, a, err, st);
     return e == cudaSuccess ? TSS_OK : TSS_CUDA_ERROR;
 }

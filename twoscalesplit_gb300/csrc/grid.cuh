@@ -9,9 +9,11 @@
 // a cell is then fixed to ascending id, which makes the result independent of the
 // atomic order and equal to a stable sort by cell of an id-ascending list.
 //
-//   k_grid_keys     key[i] = cell(pos[i]); rank[i] = atomicAdd(&count[cell], 1)
-//   k_grid_scan     off = exclusive_scan(count) in one pass (decoupled look-back);
-//                   count is zeroed for the next build; off[C] = n
+//   k_grid_keys     key[i] = cell(pos[i]); rank[i] = atomicAdd(&count[cell], 1);
+//                   per tile of kScanTile cells, the number of particles
+//                   (warp-aggregated atomics), so the scan needs no look-back
+//   k_grid_scan     off = exclusive_scan(count): each tile adds the sums of the
+//                   tiles before it; count is zeroed for the next build; off[C] = n
 //   k_grid_scatter  perm[off[key[i]] + rank[i]] = (i, id[i])
 //   k_grid_reorder  each sorted slot counts the smaller ids of its cell to find its
 //                   final place and gathers the particle's state there (SoA reorder)
@@ -31,7 +33,7 @@ struct GridBufs {
     int* key;               // [cap] cell of list entry i
     int* rank;              // [cap]
     int2* perm;             // [cap] (list index, id) in cell order (atomic order inside a cell)
-    unsigned long long* tile_state;  // [ceil(C / kScanTile)]
+    unsigned* tile_sum;     // [ntiles] particles per tile of kScanTile cells (zero between builds)
     int ntiles;
 };
 
@@ -56,17 +58,17 @@ struct ReorderArgs {
 
 __global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restrict__ n_ptr, float ox, float oy,
                             float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
-                            int* __restrict__ rank);
-__global__ void k_grid_scan(GridBufs g, int* tile_ctr, unsigned* err);
+                            int* __restrict__ rank, unsigned* __restrict__ tile_sum);
+__global__ void k_grid_scan(GridBufs g);
 __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
                                unsigned* err);
 __global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err);
 
-// Enqueue a whole build: clears the scan's tile states and `tile_ctr` (a device
-// int), then keys, scan, scatter, reorder.  `n_ptr` is a device int <= cap.
+// Enqueue a whole build: clears the tile sums, then keys, scan, scatter, reorder.
+// `n_ptr` is a device int <= cap; inconsistent offsets set kErrTimeout in *err.
 cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
-                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, int* tile_ctr,
-                               unsigned* err, cudaStream_t stream);
+                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
+                               cudaStream_t stream);
 
 size_t grid_bufs_bytes(int cap, int ncells);
 GridBufs grid_bufs_carve(void* base, int cap, int ncells);

@@ -68,7 +68,7 @@ struct tss_solver {
     Counters* cnt = nullptr;
     uint8_t* split_flag = nullptr;
     int32_t* split_ids = nullptr;
-    unsigned long long* split_tiles = nullptr;
+    unsigned* split_tile = nullptr;
     int split_ntiles = 1;
     float2* relax_pos = nullptr;
     float2* relax_vel = nullptr;
@@ -123,7 +123,7 @@ struct tss_solver {
         v.cnt = cnt;
         v.split_flag = split_flag;
         v.split_ids = split_ids;
-        v.split_tiles = split_tiles;
+        v.split_tile = split_tile;
         v.relax_pos = relax_pos;
         v.relax_vel = relax_vel;
         v.nL = nL;
@@ -164,10 +164,10 @@ struct tss_solver {
         if ((e = mark(0, s)) != cudaSuccess) return e;
         // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid)
         e = grid_build_enqueue(H.npos, H.nid, &cnt->cur[1], capH, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], H.g,
-                               reorder_args(H, true), &cnt->tile_ctr[0], &cnt->err, s);
+                               reorder_args(H, true), &cnt->err, s);
         if (e != cudaSuccess || (e = mark(1, s)) != cudaSuccess) return e;
         e = grid_build_enqueue(L.npos, L.nid, &cnt->cur[0], nL, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], L.g,
-                               reorder_args(L, false), &cnt->tile_ctr[1], &cnt->err, s);
+                               reorder_args(L, false), &cnt->err, s);
         if (e != cudaSuccess || (e = mark(2, s)) != cudaSuccess) return e;
         // 2. relaxation of last step's children (older snapshot's relaxTransient)
         for (int it = 0; it < P.relax_iters; ++it) {
@@ -181,10 +181,9 @@ struct tss_solver {
         if ((e = mark(4, s)) != cudaSuccess) return e;
         k_density_low<<<blocksL, 256, 0, s>>>(P, V);
         if ((e = mark(5, s)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
         k_force_low<<<blocksL, 256, 0, s>>>(P, V);
         if ((e = mark(6, s)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(split_tiles, 0, sizeof(unsigned long long) * split_ntiles, s)) != cudaSuccess)
-            return e;
         k_split<<<split_ntiles, kSplitThreads, 0, s>>>(P, V);
         if ((e = mark(7, s)) != cudaSuccess) return e;
         k_force_high<<<blocksH, 256, 0, s>>>(P, V);
@@ -221,9 +220,19 @@ __global__ void k_set_counts(Counters* c, int nL, int nH) {
     c->cur[0] = c->next[0] = nL;
     c->cur[1] = c->next[1] = nH;
     c->h_state0 = 0;
-    for (int k = 0; k < 8; ++k) c->tile_ctr[k] = 0;
 }
 __global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
+
+// Largest x with sqrtf(x) <= r (le) or sqrtf(x) < r (lt).  IEEE square root is
+// correctly rounded and monotone on the host and (with -prec-sqrt=true) on the
+// device, so `x <= T` decides a cutoff test exactly without taking the root.
+float sq_cutoff(float r, bool inclusive) {
+    auto ok = [&](float x) { return inclusive ? std::sqrt(x) <= r : std::sqrt(x) < r; };
+    float x = r * r;
+    while (ok(std::nextafter(x, INFINITY))) x = std::nextafter(x, INFINITY);
+    while (x > 0.0f && !ok(x)) x = std::nextafter(x, 0.0f);
+    return x;
+}
 
 bool finite_cfg(const tss_config* c) {
     const float v[] = {c->domain_origin[0], c->domain_origin[1], c->domain_end[0], c->domain_end[1], c->r_low,
@@ -349,6 +358,10 @@ tss_status tss_solver_create(const tss_config* cfg, int n_low, const float* low_
     P.slotsL = s->slotsL;
     P.slotsH = s->slotsH;
     P.capH = cap_high;
+    P.Tle_r = sq_cutoff(P.r, true);
+    P.Tlt_r = sq_cutoff(P.r, false);
+    P.Tle_rh = sq_cutoff(P.rh, true);
+    P.Tlt_rh = sq_cutoff(P.rh, false);
 
     // ---- one arena for everything ----
     Arena A;
@@ -389,7 +402,7 @@ tss_status tss_solver_create(const tss_config* cfg, int n_low, const float* low_
     A.add(&s->split_flag, n_low);
     A.add(&s->split_ids, n_low);
     s->split_ntiles = n_low > 0 ? (n_low + kSplitTile - 1) / kSplitTile : 1;
-    A.add(&s->split_tiles, s->split_ntiles);
+    A.add(&s->split_tile, s->split_ntiles);
     A.add(&s->relax_pos, s->carry ? cap_high : 1);
     A.add(&s->relax_vel, s->carry ? cap_high : 1);
     cudaError_t e = cudaMalloc(&s->arena, A.total());
@@ -432,7 +445,7 @@ tss_status tss_solver_create(const tss_config* cfg, int n_low, const float* low_
         a.dst_pos = s->wpos;
         if (e == cudaSuccess)
             e = grid_build_enqueue(wraw, wid, nW_dev, n_wall, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], gw, a,
-                                   &s->cnt->tile_ctr[2], &s->cnt->err, st);
+                                   &s->cnt->err, st);
     } else if (e == cudaSuccess) {
         // no walls: offsets all zero (already zeroed)
     }
@@ -471,7 +484,7 @@ tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
             return s->cuda_fail(e, "instantiate");
         }
     }
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
     for (int k = 0; k < n_steps; ++k)
         if ((e = cudaGraphLaunch(s->exec, st)) != cudaSuccess) return s->cuda_fail(e, "graph launch");
     s->uploaded[0] = s->uploaded[1] = false;

@@ -31,23 +31,28 @@ __global__ void __launch_bounds__(256) k_density_high(Params P, StepView V) {
         int csx, csy, cex, cey;
         grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
         grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimH[0];
-            const int b = H.off[row + cex + 1];
-            for (int j = H.off[row + csx]; j < b; ++j) {
-                if (!lamHH(s, H.st[j])) continue;
-                float dist = vnorm(sub(p, H.pos[j]));
-                if (dist <= P.rh) d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+        {
+            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamHH(s, H.st[k])) return false;
+                    x = sq(sub(p, H.pos[k]));
+                    return x <= P.Tle_rh;
+                });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
             }
         }
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int b = L.off[row + cex + 1];
-            if (P.q1) {
-                // The reference reads the HIGH sorted list at LOW-grid ranges; past
-                // n_high that list still holds its initial identity (slot t at t).
+        if (P.q1) {
+            // The reference reads the HIGH sorted list at LOW-grid ranges; past
+            // n_high that list still holds its initial identity (slot t at t).
+            for (int cy = csy; cy <= cey; ++cy) {
+                const int row = cy * P.dimL[0];
+                const int b = L.off[row + cex + 1];
                 for (int t = L.off[row + csx]; t < b; ++t) {
                     float2 pj = make_float2(0.0f, 0.0f);
                     unsigned sj = 0;
@@ -62,15 +67,25 @@ __global__ void __launch_bounds__(256) k_density_high(Params P, StepView V) {
                         }
                     }
                     if (!lamHL(s, sj)) continue;
-                    float dist = vnorm(sub(p, pj));
-                    if (dist <= P.rh) d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                    const float x = sq(sub(p, pj));
+                    if (x <= P.Tle_rh) {
+                        const float dist = sqrtf(x);
+                        d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                    }
                 }
-            } else {
-                for (int t = L.off[row + csx]; t < b; ++t) {
-                    if (!lamHL(s, L.st[t])) continue;
-                    float dist = vnorm(sub(p, L.pos[t]));
-                    if (dist <= P.rh) dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
-                }
+            }
+        } else {
+            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamHL(s, L.st[k])) return false;
+                    x = sq(sub(p, L.pos[k]));
+                    return x <= P.Tle_rh;
+                });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
             }
         }
         d *= P.mH;
@@ -99,25 +114,33 @@ __global__ void __launch_bounds__(256) k_density_low(Params P, StepView V) {
         int csx, csy, cex, cey;
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int b = L.off[row + cex + 1];
-            for (int j = L.off[row + csx]; j < b; ++j) {
-                float dist = vnorm(sub(p, L.pos[j]));
-                if (dist <= P.r) d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+        {
+            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    x = sq(sub(p, L.pos[k]));
+                    return x <= P.Tle_r;
+                });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
             }
         }
         if (cross) {
             grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
             grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-            for (int cy = csy; cy <= cey; ++cy) {
-                const int row = cy * P.dimH[0];
-                const int b = H.off[row + cex + 1];
-                for (int j = H.off[row + csx]; j < b; ++j) {
-                    if (!lamLH(s, H.st[j])) continue;
-                    float dist = vnorm(sub(p, H.pos[j]));
-                    if (dist <= P.r) dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
-                }
+            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamLH(s, H.st[k])) return false;
+                    x = sq(sub(p, H.pos[k]));
+                    return x <= P.Tle_r;
+                });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
             }
         }
         d *= P.mL;
@@ -131,112 +154,141 @@ __global__ void __launch_bounds__(256) k_density_low(Params P, StepView V) {
     }
 }
 
+// Wall term of a force sum (updateAccCell 562-579 / updateAccCellComplementHigh
+// 867-884): every wall particle of the window's cells, in cell order.  Pairs with
+// sqrtf(x) > rad have q >= 2 and add exactly zero, so they are skipped.
+__device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, float2 p, int csx, int cex, int csy,
+                                           int cey, float rad, float Tle, float cB) {
+    float2 accB = make_float2(0.f, 0.f);
+    for (int cy = csy; cy <= cey; ++cy) {
+        const int row = cy * P.dimL[0];
+        const int wb = V.woff[row + cex + 1];
+        for (int k = V.woff[row + csx]; k < wb; ++k) {
+            const float2 pik = sub(p, V.wpos[k]);
+            const float x = sq(pik);
+            if (!(x <= Tle)) continue;
+            const float gm = wall_weight(sqrtf(x), rad, P.cs);
+            accB.x += cB * gm * pik.x;
+            accB.y += cB * gm * pik.y;
+        }
+    }
+    return accB;
+}
+
 // ---------------------------------------------------------------------------
 // Low-res force + advance + split test: computeParticleAcceleration
 // (WCSPHSolver.cu:1648-1865) with advance (1604-1646) fused; its predicted position
-// is the advanced position bit for bit.
+// is the advanced position bit for bit.  The fluid and wall sums are independent
+// accumulators, so they are taken in two passes over the window.  Each warp adds
+// its split count to the tile counter the compaction reads.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_force_low(Params P, StepView V) {
     const int n = V.cnt->cur[0];
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     const bool cross = V.cnt->h_state0 != 0;
-    for (int i = tid(); i < n; i += nthreads()) {
-        float2 p = L.pos[i], v = L.vel[i];
-        const unsigned s = L.st[i];
-        const float dens = L.dens[i], qi = L.q[i];
-        float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f);
-        float2 accT = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
-        int csx, csy, cex, cey;
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int b = L.off[row + cex + 1];
-            for (int j = L.off[row + csx]; j < b; ++j) {
-                const float2 pij = sub(p, L.pos[j]);
-                const float dist = vnorm(pij);
-                if (dist != 0.0f && dist < P.r) {
-                    if (!notDeleted(L.st[j])) continue;
-                    pair_force(P, pij, dist, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        bool flag = false;
+        if (i < n) {
+            float2 p = L.pos[i], v = L.vel[i];
+            const unsigned s = L.st[i];
+            const float dens = L.dens[i], qi = L.q[i];
+            float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
+            int csx, csy, cex, cey;
+            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+            {
+                Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+                float2 pij = make_float2(0.f, 0.f);
+                float x = 0.0f;
+                for (;;) {
+                    const int j = w.next([&](int k) {
+                        pij = sub(p, L.pos[k]);
+                        x = sq(pij);
+                        return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
+                    });
+                    if (j < 0) break;
+                    pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
                 }
             }
-            const int wb = V.woff[row + cex + 1];
-            for (int k = V.woff[row + csx]; k < wb; ++k) {
-                const float2 pik = sub(p, V.wpos[k]);
-                const float gm = wall_weight(vnorm(pik), P.r, P.cs);
-                accB.x += P.cBL * gm * pik.x;
-                accB.y += P.cBL * gm * pik.y;
-            }
-        }
-        if (cross) {
-            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-            for (int cy = csy; cy <= cey; ++cy) {
-                const int row = cy * P.dimH[0];
-                const int b = H.off[row + cex + 1];
-                for (int j = H.off[row + csx]; j < b; ++j) {
-                    if (!lamLH(s, H.st[j])) continue;
-                    const float2 pij = sub(p, H.pos[j]);
-                    const float dist = vnorm(pij);
-                    if (dist != 0.0f && dist < P.r)
-                        pair_force(P, pij, dist, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
+            const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
+            if (cross) {
+                grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+                grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+                Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+                float2 pij = make_float2(0.f, 0.f);
+                float x = 0.0f;
+                for (;;) {
+                    const int j = w.next([&](int k) {
+                        if (!lamLH(s, H.st[k])) return false;
+                        pij = sub(p, H.pos[k]);
+                        x = sq(pij);
+                        return x != 0.0f && x <= P.Tlt_r;
+                    });
+                    if (j < 0) break;
+                    pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
                 }
             }
+            acc.x *= -P.mL;
+            acc.y *= -P.mL;
+            accH.x *= -P.mH;
+            accH.y *= -P.mH;
+            acc.x += accH.x;
+            acc.y += accH.y;
+            acc.x -= P.sigma * accT.x;
+            acc.y -= P.sigma * accT.y;
+            acc.x += accB.x;
+            acc.y += accB.y;
+            acc.y -= P.g;
+            L.acc[i] = acc;
+            if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+            v.x += P.dt * acc.x;
+            v.y += P.dt * acc.y;
+            p.x += P.dt * v.x;
+            p.y += P.dt * v.y;
+            L.npos[i] = p;
+            L.nvel[i] = v;
+            L.nid[i] = L.id[i];
+            uint8_t ns = static_cast<uint8_t>(s);
+            if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
+                ns = 1;
+                flag = true;
+            }
+            L.nst[i] = ns;
+            V.split_flag[i] = flag ? 1 : 0;
+            if (L.ndens) {
+                L.ndens[i] = dens;
+                L.npres[i] = L.pres[i];
+            }
         }
-        acc.x *= -P.mL;
-        acc.y *= -P.mL;
-        accH.x *= -P.mH;
-        accH.y *= -P.mH;
-        acc.x += accH.x;
-        acc.y += accH.y;
-        acc.x -= P.sigma * accT.x;
-        acc.y -= P.sigma * accT.y;
-        acc.x += accB.x;
-        acc.y += accB.y;
-        acc.y -= P.g;
-        L.acc[i] = acc;
-        if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
-        v.x += P.dt * acc.x;
-        v.y += P.dt * acc.y;
-        p.x += P.dt * v.x;
-        p.y += P.dt * v.y;
-        L.npos[i] = p;
-        L.nvel[i] = v;
-        L.nid[i] = L.id[i];
-        uint8_t ns = static_cast<uint8_t>(s);
-        uint8_t flag = 0;
-        if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
-            ns = 1;
-            flag = 1;
-        }
-        L.nst[i] = ns;
-        V.split_flag[i] = flag;
-        if (L.ndens) {
-            L.ndens[i] = dens;
-            L.npres[i] = L.pres[i];
-        }
+        // a warp's 32 particles lie in one compaction tile (kSplitTile % 32 == 0)
+        const unsigned m = __ballot_sync(0xffffffffu, flag);
+        if (lane == 0 && m) atomicAdd(&V.split_tile[(base + (threadIdx.x & ~31)) / kSplitTile], __popc(m));
     }
 }
 
 // ---------------------------------------------------------------------------
-// Ordered stream compaction of the split flags (warp ballot + block scan +
-// decoupled look-back) and creation of the 4 children of each split
-// (initSubParticlesAndAddToList, WCSPHSolver.cu:956-1005): children of the k-th
-// split parent (in sorted order) take high-res list entries n_high + 4k + 0..3.
+// Ordered stream compaction of the split flags (warp ballots + block scan; the
+// tile's offset is the sum of the earlier tiles' counts that k_force_low left)
+// and creation of the 4 children of each split (initSubParticlesAndAddToList,
+// WCSPHSolver.cu:956-1005): children of the k-th split parent in sorted order
+// take high-res list entries n_high + 4k + 0..3.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
-    __shared__ int s_tile;
     __shared__ unsigned s_warp[kSplitThreads / 32];
-    __shared__ unsigned s_prefix;
-    if (threadIdx.x == 0) s_tile = atomicAdd(&V.cnt->tile_ctr[7], 1);
-    __syncthreads();
-    const int tile = s_tile;
+    __shared__ unsigned s_red[kSplitThreads / 32];
+    const int tile = blockIdx.x;
     const int n = V.cnt->cur[0];
     const int nH = V.cnt->cur[1];
-    const int ntiles = max(1, (n + kSplitTile - 1) / kSplitTile);
-    if (tile >= ntiles) return;
+    const int ntiles = gridDim.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned before = 0;
+    for (int t = threadIdx.x; t < tile; t += blockDim.x) before += V.split_tile[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) s_red[warp] = before;
     // warp-striped items: item k of lane l of warp w is tile base + (w*K + k)*32 + l,
     // so each warp's ballots cover 32 consecutive particles in order
     const int wbase = tile * kSplitTile + warp * kSplitItems * 32;
@@ -253,64 +305,60 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
     __syncthreads();
     if (warp == 0) {
         unsigned w = lane < kSplitThreads / 32 ? s_warp[lane] : 0u;
+        unsigned r = lane < kSplitThreads / 32 ? s_red[lane] : 0u;
         unsigned wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
             if (lane >= o) wi += t;
         }
-        if (lane < kSplitThreads / 32) s_warp[lane] = wi - w;
-        const unsigned total = __shfl_sync(0xffffffffu, wi, kSplitThreads / 32 - 1);
-        const unsigned prefix = lookback_prefix(V.split_tiles, tile, total, &V.cnt->err);
-        if (lane == 0) {
-            s_prefix = prefix;
-            if (tile == ntiles - 1) {
-                const int nsplit = static_cast<int>(prefix + total);
-                long long want = static_cast<long long>(nH) + 4LL * nsplit;
-                V.cnt->n_split = nsplit;
-                if (want > P.capH) {
-                    atomicOr(&V.cnt->err, kErrCapacity);
-                    want = nH + 4LL * ((P.capH - nH) / 4);
-                }
-                V.cnt->next[1] = static_cast<int>(want);
-                V.cnt->next[0] = n;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (lane < kSplitThreads / 32) s_warp[lane] = wi - w + r;
+        const unsigned total = __shfl_sync(0xffffffffu, wi, kSplitThreads / 32 - 1) + r;
+        if (lane == 0 && tile == ntiles - 1) {
+            const int nsplit = static_cast<int>(total);
+            long long want = static_cast<long long>(nH) + 4LL * nsplit;
+            V.cnt->n_split = nsplit;
+            if (want > P.capH) {
+                atomicOr(&V.cnt->err, kErrCapacity);
+                want = nH + 4LL * ((P.capH - nH) / 4);
             }
+            V.cnt->next[1] = static_cast<int>(want);
+            V.cnt->next[0] = n;
         }
     }
     __syncthreads();
-    unsigned rank = s_prefix + s_warp[warp];
+    unsigned rank = s_warp[warp];
     const unsigned lt = (1u << lane) - 1u;
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < kSplitItems; ++k) {
         const unsigned m = masks[k];
         if (m & (1u << lane)) {
             const int i = wbase + k * 32 + lane;
             const unsigned r = rank + __popc(m & lt);
-            if (r >= static_cast<unsigned>(n)) {  // only after a failed look-back
-                atomicOr(&V.cnt->err, kErrTimeout);
-                rank += __popc(m);
-                continue;
-            }
-            const int id = V.L.id[i];
-            V.split_ids[r] = id;
-            const long long hb = static_cast<long long>(nH) + 4LL * r;
-            if (hb + 4 <= P.capH) {
-                const float2 p = V.L.npos[i], v = V.L.nvel[i];
-                const float rho = V.L.dens[i];
-                const float rad = static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) /
-                                                                 (static_cast<double>(2.0f * rho) * kPi)));
-                const float2 cp[4] = {make_float2(p.x + rad, p.y + rad), make_float2(p.x - rad, p.y + rad),
-                                      make_float2(p.x + rad, p.y - rad), make_float2(p.x - rad, p.y - rad)};
+            if (r < static_cast<unsigned>(n)) {
+                const int id = V.L.id[i];
+                V.split_ids[r] = id;
+                const long long hb = static_cast<long long>(nH) + 4LL * r;
+                if (hb + 4 <= P.capH) {
+                    const float2 p = V.L.npos[i], v = V.L.nvel[i];
+                    const float rho = V.L.dens[i];
+                    const float rad = static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) /
+                                                                     (static_cast<double>(2.0f * rho) * kPi)));
+                    const float2 cp[4] = {make_float2(p.x + rad, p.y + rad), make_float2(p.x - rad, p.y + rad),
+                                          make_float2(p.x + rad, p.y - rad), make_float2(p.x - rad, p.y - rad)};
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const int h = static_cast<int>(hb) + c;
-                    V.H.npos[h] = cp[c];
-                    V.H.nvel[h] = v;
-                    V.H.nst[h] = 1;
-                    V.H.nid[h] = 4 * id + c;
-                    if (V.H.ndens) {
-                        V.H.ndens[h] = 0.0f;
-                        V.H.npres[h] = 0.0f;
+                    for (int c = 0; c < 4; ++c) {
+                        const int h = static_cast<int>(hb) + c;
+                        V.H.npos[h] = cp[c];
+                        V.H.nvel[h] = v;
+                        V.H.nst[h] = 1;
+                        V.H.nid[h] = 4 * id + c;
+                        if (V.H.ndens) {
+                            V.H.ndens[h] = 0.0f;
+                            V.H.npres[h] = 0.0f;
+                        }
                     }
                 }
             }
@@ -333,43 +381,44 @@ __global__ void __launch_bounds__(256) k_force_high(Params P, StepView V) {
         float2 p = H.pos[i], v = H.vel[i];
         const unsigned s = H.st[i];
         const float dens = H.dens[i], qi = H.q[i];
-        float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f);
-        float2 accT = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
+        float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
         int csx, csy, cex, cey;
         grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
         grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimH[0];
-            const int b = H.off[row + cex + 1];
-            for (int j = H.off[row + csx]; j < b; ++j) {
-                if (!lamHH(s, H.st[j])) continue;
-                const float2 pij = sub(p, H.pos[j]);
-                const float dist = vnorm(pij);
-                if (dist != 0.0f && dist < P.rh)
-                    pair_force(P, pij, dist, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
+        {
+            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+            float2 pij = make_float2(0.f, 0.f);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamHH(s, H.st[k])) return false;
+                    pij = sub(p, H.pos[k]);
+                    x = sq(pij);
+                    return x != 0.0f && x <= P.Tlt_rh;
+                });
+                if (j < 0) break;
+                pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
             }
         }
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int b = L.off[row + cex + 1];
-            for (int j = L.off[row + csx]; j < b; ++j) {
-                const unsigned sj = L.nst[j];
-                if (!(lamHL(s, sj) && notDeleted(sj))) continue;
-                const float2 pij = sub(p, L.pos[j]);
-                const float dist = vnorm(pij);
-                if (dist != 0.0f && dist < P.r)
-                    pair_force(P, pij, dist, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
-            }
-            const int wb = V.woff[row + cex + 1];
-            for (int k = V.woff[row + csx]; k < wb; ++k) {
-                const float2 pik = sub(p, V.wpos[k]);
-                const float gm = wall_weight(vnorm(pik), P.rh, P.cs);
-                accB.x += P.cBH * gm * pik.x;
-                accB.y += P.cBH * gm * pik.y;
+        {
+            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+            float2 pij = make_float2(0.f, 0.f);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    const unsigned sj = L.nst[k];
+                    if (!(lamHL(s, sj) && notDeleted(sj))) return false;
+                    pij = sub(p, L.pos[k]);
+                    x = sq(pij);
+                    return x != 0.0f && x <= P.Tlt_r;
+                });
+                if (j < 0) break;
+                pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
             }
         }
+        const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
         acc.x *= -P.mH;
         acc.y *= -P.mH;
         accL.x *= -P.mL;
@@ -550,7 +599,6 @@ __global__ void k_step_finish(Counters* c) {
         c->n_fresh = c->n_split;
         c->h_state0 = 0;
         c->steps += 1;
-        for (int k = 0; k < 8; ++k) c->tile_ctr[k] = 0;
     }
 }
 

@@ -33,7 +33,7 @@ struct StepView {
     Counters* cnt;
     uint8_t* split_flag;    // [n_low]
     int32_t* split_ids;     // [n_low] parents split this step (= next step's fresh list)
-    unsigned long long* split_tiles;
+    unsigned* split_tile;   // [ceil(n_low / kSplitTile)] splits per tile, zero at step start
     float2* relax_pos;      // [capH] relaxation scratch
     float2* relax_vel;
     int nL;                 // low-res count (constant for a solver)

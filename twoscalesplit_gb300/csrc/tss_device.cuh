@@ -14,10 +14,7 @@ constexpr double kPi = 3.14159265358979323846;  // WCSPHSolver.cu:19
 // error word bits (mirror TSS_ERR_* in include/tss.h)
 constexpr unsigned kErrCapacity = 0x1u;
 constexpr unsigned kErrNumeric = 0x2u;
-constexpr unsigned kErrTimeout = 0x4u;
-
-// Spin limit for decoupled look-back waits; ~0.5 s with the back-off below.
-constexpr int kSpinLimit = 1 << 22;
+constexpr unsigned kErrTimeout = 0x4u;  // inconsistent grid offsets (no device-side wait exists)
 
 struct Params {
     float ox, oy;
@@ -33,6 +30,10 @@ struct Params {
     int q1;
     int slotsL, slotsH;    // slot-id spaces: low ids < slotsL, high ids < slotsH = 4*slotsL
     int capH;
+    // exact squared-distance cutoffs: x <= Tle_s  <=>  sqrtf(x) <= r_s and
+    // x <= Tlt_s  <=>  sqrtf(x) < r_s, for x = dx*dx + dy*dy (IEEE sqrt is monotone
+    // and correctly rounded, so these are the largest floats with that property)
+    float Tle_r, Tlt_r, Tle_rh, Tlt_rh;
 };
 
 // Device-side counters of one solver.  `cur` is what this step's kernels use;
@@ -46,7 +47,6 @@ struct Counters {
     int h_state0;    // 1 if some high-res particle has (state & 1) == 0
     long long steps;
     int sorted[2];   // particles sorted in the last step (its `cur` counts)
-    int tile_ctr[8]; // tile claim counters for the look-back passes of one step
 };
 
 __device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating
@@ -140,63 +140,42 @@ __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float di
     accT.y += pij.y * (w + w2) / 2.0f;
 }
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-// Decoupled look-back (single-pass prefix over tiles).  Called by all 32 lanes of
-// warp 0 of the block owning `tile`; publishes the tile's aggregate, walks back
-// over predecessors 32 at a time, publishes the inclusive prefix and returns the
-// exclusive prefix (in every lane).  Status word: flag << 32 | value, flag 1 =
-// aggregate only, 2 = inclusive prefix.  Waits are bounded: after kSpinLimit polls
-// the error word gets kErrTimeout and the tile proceeds with what it has.
-__device__ __forceinline__ unsigned lookback_prefix(unsigned long long* state, int tile, unsigned aggregate,
-                                                    unsigned* err) {
-    const int lane = threadIdx.x & 31;
-    if (tile == 0) {
-        if (lane == 0) st_release_u64(&state[0], (2ull << 32) | aggregate);
-        return 0u;
+// Candidates of a cell window, row by row (cells in x order, particles in cell
+// order: the reference's summation order).  next() returns the next candidate that
+// `accept` takes, or -1.  Each lane skips rejected candidates on its own and the
+// search loop has a single exit, so the lanes meet again before the caller's pair
+// arithmetic, which then runs with the warp converged instead of at the in-range
+// fraction of the lanes.
+struct Window {
+    const int* off;
+    int dimx, csx, cex, cy, cey, j, b;
+    __device__ __forceinline__ Window(const int* off_, int dimx_, int csx_, int cex_, int csy_, int cey_)
+        : off(off_), dimx(dimx_), csx(csx_), cex(cex_), cy(csy_), cey(cey_) {
+        const int row = cy * dimx;
+        j = off[row + csx];
+        b = off[row + cex + 1];
     }
-    if (lane == 0) st_release_u64(&state[tile], (1ull << 32) | aggregate);
-    unsigned prefix = 0;
-    int window = tile - 1;
-    while (true) {
-        int t = window - lane;
-        unsigned long long w = 2ull << 32;  // before tile 0: an inclusive zero
-        if (t >= 0) {
-            int spins = 0;
-            while (true) {
-                w = ld_acquire_u64(&state[t]);
-                if ((w >> 32) != 0) break;
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, kErrTimeout);
-                    w = 2ull << 32;
-                    break;
-                }
-                __nanosleep(64);
+    template <class Accept>
+    __device__ __forceinline__ int next(Accept&& accept) {
+        int found = -1;
+        while (true) {
+            if (j >= b) {
+                if (++cy > cey) break;
+                const int row = cy * dimx;
+                j = off[row + csx];
+                b = off[row + cex + 1];
+                continue;
+            }
+            const int k = j++;
+            if (accept(k)) {
+                found = k;
+                break;
             }
         }
-        unsigned flag = unsigned(w >> 32);
-        unsigned val = unsigned(w);
-        unsigned inc_mask = __ballot_sync(0xffffffffu, flag == 2u);
-        if (inc_mask) {
-            int stop = __ffs(inc_mask) - 1;  // closest predecessor with an inclusive prefix
-            unsigned contrib = lane <= stop ? val : 0u;
-            for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
-            prefix += contrib;
-            break;
-        }
-        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-        prefix += val;
-        window -= 32;
+        return found;
     }
-    if (lane == 0) st_release_u64(&state[tile], (2ull << 32) | (prefix + aggregate));
-    return prefix;
-}
+};
+
+__device__ __forceinline__ float sq(float2 v) { return v.x * v.x + v.y * v.y; }
 
 }  // namespace tss

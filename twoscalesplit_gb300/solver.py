@@ -54,7 +54,7 @@ class Solver:
         check(st, self.h, self.lib)
 
     def step(self, n=1, stream=None):
-        """Enqueue n steps; stream is a cudaStream_t handle (int) or None."""
+        """Enqueue n steps on a cudaStream_t handle (int; None or 0 = the default stream)."""
         self._check(self.lib.tss_solver_step(self.h, int(n), ctypes.c_void_p(stream) if stream else None))
 
     def sync(self):

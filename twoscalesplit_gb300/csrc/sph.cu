@@ -166,7 +166,7 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
         for (int k = V.woff[row + csx]; k < wb; ++k) {
             const float2 pik = sub(p, V.wpos[k]);
             const float x = sq(pik);
-            if (!(x <= Tle)) continue;
+            if (x > Tle) continue;  // NaN passes: the reference's 0 * NaN offset propagates it
             const float gm = wall_weight(sqrtf(x), rad, P.cs);
             accB.x += cB * gm * pik.x;
             accB.y += cB * gm * pik.y;

@@ -212,6 +212,28 @@ tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, int n,
                           int dimx, int dimy, int32_t* d_order, int32_t* d_cell_off,
                           void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* Grid build that allocates nothing.  No counterpart in the reference: it is
+ * tss_grid_build with its scratch in a fixed array inside this library, for callers
+ * that may not call cudaMalloc/cudaFree (a host application's per-frame callback,
+ * where those calls can stall the whole device, or a plug-in whose device memory is
+ * owned by its host's memory manager).  The caller still passes d_pos, d_id,
+ * d_order and d_cell_off as for tss_grid_build.
+ *   - Limit: tss_grid_workspace_size(n, dimx, dimy) must not exceed
+ *     TSS_GRID_NOALLOC_MAX_BYTES (32 MiB, e.g. 500,000 particles on a 1400x1400
+ *     grid); larger problems get TSS_CAPACITY and should use tss_grid_build.
+ *   - The array occupies TSS_GRID_NOALLOC_MAX_BYTES on every GPU that loads the
+ *     library, until the process exits.
+ *   - The first call on a device looks up the array's device address on that
+ *     device; make that first call before any stream capture.
+ *   - All calls share the array: calls whose work overlaps on the GPU (other
+ *     streams, other host threads) race and give undefined results.  Each call
+ *     clears the parts that must start at zero. */
+#define TSS_GRID_NOALLOC_MAX_BYTES (32u << 20)
+tss_status tss_grid_build_noalloc(const float* d_pos, const int32_t* d_id, int n,
+                                  float origin_x, float origin_y, float cell_size,
+                                  int dimx, int dimy, int32_t* d_order, int32_t* d_cell_off,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,7 @@ STAGE_NAMES = ["grid_high", "grid_low", "relax", "density_high", "density_low", 
                "force_high"]
 
 TSS_ERR_CAPACITY = 0x1
+TSS_GRID_NOALLOC_MAX_BYTES = 32 << 20
 TSS_ERR_NUMERIC = 0x2
 TSS_ERR_TIMEOUT = 0x4
 
@@ -166,6 +167,7 @@ def load_library(path=None):
         "tss_status_string": (ctypes.c_char_p, [i]),
         "tss_grid_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
         "tss_grid_build": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp, ctypes.c_size_t, vp]),
+        "tss_grid_build_noalloc": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

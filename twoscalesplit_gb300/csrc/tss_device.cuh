@@ -66,45 +66,38 @@ __device__ __forceinline__ int cell_hash(float2 p, float ox, float oy, float cel
     return cy * dimx + cx;
 }
 
-// evaluateM4Kernel(High), WCSPHSolver.cu:116-160
+// evaluateM4Kernel(High), WCSPHSolver.cu:116-160.  Both polynomial branches are
+// evaluated and one is selected: each branch's expression keeps the reference's
+// association, so the selected value is the reference's bit for bit, and a warp
+// whose lanes fall into different branches does not run both in turn.
 __device__ __forceinline__ float kernW(float d, float rad, float C) {
-    float q = d * 2.0f / rad;
-    if (q < 1.0f) {
-        float a = 2.0f - q, b = 1.0f - q;
-        return C * (a * a * a - 4.0f * b * b * b);
-    } else if (q < 2.0f) {
-        float a = 2.0f - q;
-        return C * a * a * a;
-    }
-    return 0.0f;
+    const float q = d * 2.0f / rad;
+    const float a = 2.0f - q, b = 1.0f - q;
+    const float w1 = C * (a * a * a - 4.0f * b * b * b);
+    const float w2 = C * a * a * a;
+    return q < 1.0f ? w1 : (q < 2.0f ? w2 : 0.0f);
 }
 
-// evaluateGradientM4Kernel(High), WCSPHSolver.cu:162-239
+// evaluateGradientM4Kernel(High), WCSPHSolver.cu:162-239: c = G*(a*a - 4*b*b)/d for
+// q < 1 and c = G*a*a/d for q < 2 -- one division of the selected numerator.
 __device__ __forceinline__ float2 kernDW(float2 x, float d, float rad, float G) {
-    float q = d * 2.0f / rad;
-    if (q < 1.0f) {
-        float a = 2.0f - q, b = 1.0f - q;
-        float c = G * (a * a - 4.0f * b * b) / d;
-        return make_float2(c * x.x, c * x.y);
-    } else if (q < 2.0f) {
-        float a = 2.0f - q;
-        float c = G * a * a / d;
-        return make_float2(c * x.x, c * x.y);
-    }
-    return make_float2(0.0f, 0.0f);
+    const float q = d * 2.0f / rad;
+    const float a = 2.0f - q, b = 1.0f - q;
+    const float n1 = G * (a * a - 4.0f * b * b);
+    const float n2 = G * a * a;
+    const float c = (q < 1.0f ? n1 : n2) / d;
+    return q < 2.0f ? make_float2(c * x.x, c * x.y) : make_float2(0.0f, 0.0f);
 }
 
-// evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114
+// evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114 (selected, as above)
 __device__ __forceinline__ float wall_weight(float d, float rad, float cs) {
-    float q = d * 2.0f / rad;
-    float c = 0.02f * cs * cs / (d * d);
-    if (q < 2.0f / 3.0f) return c * 2.0f / 3.0f;
-    if (q < 1.0f) return c * (2.0f * q - 3.0f / 2.0f * q * q);
-    if (q < 2.0f) {
-        float a = 2.0f - q;
-        return c * 0.5f * a * a;
-    }
-    return 0.0f;
+    const float q = d * 2.0f / rad;
+    const float c = 0.02f * cs * cs / (d * d);
+    const float r1 = c * 2.0f / 3.0f;
+    const float r2 = c * (2.0f * q - 3.0f / 2.0f * q * q);
+    const float a = 2.0f - q;
+    const float r3 = c * 0.5f * a * a;
+    return q < 2.0f / 3.0f ? r1 : (q < 1.0f ? r2 : (q < 2.0f ? r3 : 0.0f));
 }
 
 __device__ __forceinline__ float vnorm(float2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
@@ -127,9 +120,10 @@ __device__ __forceinline__ bool notDeleted(unsigned s) { return s < 2u; }       
 // qi, qj are p/rho^2 of the two particles (the reference's pre/dens2, prej/densj2).
 __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float dist, float2 vij, float qi, float qj,
                                            float densi, float densj, float h, float2& acc, float2& accT) {
+    const float dvp = vij.x * pij.x + vij.y * pij.y;
+    const float visc = dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
     float coeff = qi + qj;
-    float dvp = vij.x * pij.x + vij.y * pij.y;
-    if (dvp < 0.0f) coeff -= dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
+    coeff = dvp < 0.0f ? coeff - visc : coeff;  // the reference's `if (dvp < 0) coeff -= ...`
     float2 gI = kernDW(pij, dist, P.r, P.GL);
     float2 gJ = kernDW(pij, dist, P.rh, P.GH);
     acc.x += coeff * (gI.x + gJ.x) / 2.0f;
@@ -149,6 +143,7 @@ __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float di
 struct Window {
     const int* off;
     int dimx, csx, cex, cy, cey, j, b;
+    __device__ __forceinline__ Window() : off(nullptr), dimx(0), csx(0), cex(0), cy(1), cey(0), j(0), b(0) {}
     __device__ __forceinline__ Window(const int* off_, int dimx_, int csx_, int cex_, int csy_, int cey_)
         : off(off_), dimx(dimx_), csx(csx_), cex(cex_), cy(csy_), cey(cey_) {
         const int row = cy * dimx;
@@ -177,5 +172,36 @@ struct Window {
 };
 
 __device__ __forceinline__ float sq(float2 v) { return v.x * v.x + v.y * v.y; }
+
+// Two-phase, warp-synchronous gather.  Phase 1: each lane walks its window and
+// writes the indices of up to kGatherK accepted candidates, in order, to its column
+// of a shared-memory list.  Phase 2: the warp runs `pair` for list entry 0, 1, ...
+// up to the longest lane's count, every lane on its own entry, so the expensive
+// pair arithmetic runs with (nearly) all lanes active; per lane the pairs are still
+// taken in window order, so every sum is the reference's.  Repeats until every
+// lane's window is exhausted.  All 32 lanes of the warp must call it (inactive
+// lanes pass active = false and an empty Window).
+constexpr int kGatherThreads = 256;
+constexpr int kGatherK = 16;
+
+template <class Accept, class Pair>
+__device__ __forceinline__ void gather(Window& w, bool active, int* col, Accept&& accept, Pair&& pair) {
+    bool more = active;
+    while (__any_sync(0xffffffffu, more)) {
+        int cnt = 0;
+        while (more && cnt < kGatherK) {
+            const int j = w.next(accept);
+            if (j < 0) {
+                more = false;
+            } else {
+                col[cnt * kGatherThreads] = j;
+                ++cnt;
+            }
+        }
+        const int maxc = __reduce_max_sync(0xffffffffu, cnt);
+        for (int k = 0; k < maxc; ++k)
+            if (k < cnt) pair(col[k * kGatherThreads]);
+    }
+}
 
 }  // namespace tss

@@ -25,29 +25,14 @@ __global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restric
                             float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
                             int* __restrict__ rank, unsigned* __restrict__ tile_sum) {
     const int n = *n_ptr;
-    const int lane = threadIdx.x & 31;
-    // warp-uniform trip count, so the ballot/match below see whole warps
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool act = i < n;
-        int c = 0;
-        if (act) {
-            c = cell_hash(pos[i], ox, oy, cell, dimx, dimy);
-            key[i] = c;
-            rank[i] = static_cast<int>(atomicAdd(&count[c], 1u));
-        }
-        const unsigned mask = __ballot_sync(0xffffffffu, act);
-        if (act) {
-            const unsigned t = static_cast<unsigned>(c) / kScanTile;
-            const unsigned peers = __match_any_sync(mask, t);
-            if (lane == __ffs(peers) - 1) atomicAdd(&tile_sum[t], static_cast<unsigned>(__popc(peers)));
-        }
-    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        grid_key(count, key, rank, tile_sum, i, cell_hash(pos[i], ox, oy, cell, dimx, dimy));
 }
 
 // One tile of kScanTile counts per block.  The tile's offset is the sum of the
-// tile sums before it (at most a few thousand, read from L2), so tiles are
-// independent and nothing waits on another block.
+// tile sums before it (a few hundred, read from L2), so tiles are independent and
+// nothing waits on another block.  Counts are zeroed for the next key pass (only
+// the 16-byte groups that hold a non-zero count are written back).
 __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
     __shared__ unsigned s_warp[kScanThreads / 32];
     __shared__ unsigned s_red[kScanThreads / 32];
@@ -63,19 +48,22 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
     unsigned v[kScanItems];
     const bool full = base + kScanItems <= C;
     if (full) {
-        const uint4* p = reinterpret_cast<const uint4*>(g.count + base);
-        uint4 a = p[0], b = p[1];
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-        uint4* q = reinterpret_cast<uint4*>(g.count + base);
-        q[0] = make_uint4(0, 0, 0, 0);
-        q[1] = make_uint4(0, 0, 0, 0);
+        uint4* p = reinterpret_cast<uint4*>(g.count + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 a = p[q];
+            v[4 * q] = a.x;
+            v[4 * q + 1] = a.y;
+            v[4 * q + 2] = a.z;
+            v[4 * q + 3] = a.w;
+            if (a.x | a.y | a.z | a.w) p[q] = make_uint4(0, 0, 0, 0);
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
             int idx = base + k;
             v[k] = idx < C ? g.count[idx] : 0u;
-            if (idx < C) g.count[idx] = 0u;
+            if (idx < C && v[k]) g.count[idx] = 0u;
         }
     }
     unsigned sum = 0;
@@ -104,23 +92,29 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
     }
     __syncthreads();
     unsigned run = s_warp[warp] + (inc - sum);
-    unsigned o8[kScanItems];
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        o8[k] = run;
-        run += v[k];
-    }
     if (full) {
         int4* q = reinterpret_cast<int4*>(g.off + base);
-        q[0] = make_int4(o8[0], o8[1], o8[2], o8[3]);
-        q[1] = make_int4(o8[4], o8[5], o8[6], o8[7]);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            int4 o4;
+            o4.x = static_cast<int>(run);
+            run += v[4 * k];
+            o4.y = static_cast<int>(run);
+            run += v[4 * k + 1];
+            o4.z = static_cast<int>(run);
+            run += v[4 * k + 2];
+            o4.w = static_cast<int>(run);
+            run += v[4 * k + 3];
+            q[k] = o4;
+        }
         if (base + kScanItems == C) g.off[C] = static_cast<int>(run);
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
             int idx = base + k;
-            if (idx < C) g.off[idx] = static_cast<int>(o8[k]);
-            if (idx == C - 1) g.off[C] = static_cast<int>(o8[k] + v[k]);
+            if (idx < C) g.off[idx] = static_cast<int>(run);
+            run += v[k];
+            if (idx == C - 1) g.off[C] = static_cast<int>(run);
         }
     }
 }
@@ -208,18 +202,35 @@ GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
     return g;
 }
 
-cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
-                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
-                               cudaStream_t stream) {
+cudaError_t grid_keys_enqueue(const float2* pos, const int* n_ptr, int cap, float ox, float oy, float cell, int dimx,
+                              int dimy, GridBufs g, cudaStream_t stream) {
+    const int T = 256;
+    k_grid_keys<<<particle_blocks(cap, T), T, 0, stream>>>(pos, n_ptr, ox, oy, cell, dimx, dimy, g.count, g.key,
+                                                           g.rank, g.tile_sum);
+    return cudaGetLastError();
+}
+
+cudaError_t grid_sort_enqueue(const int32_t* id, const int* n_ptr, int cap, GridBufs g, ReorderArgs a,
+                              unsigned* err, cudaStream_t stream) {
     const int T = 256;
     const int pb = particle_blocks(cap, T);
     cudaError_t e;
-    if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
-    k_grid_keys<<<pb, T, 0, stream>>>(pos, n_ptr, ox, oy, cell, dimx, dimy, g.count, g.key, g.rank, g.tile_sum);
     k_grid_scan<<<g.ntiles, kScanThreads, 0, stream>>>(g);
+    if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
     k_grid_scatter<<<pb, T, 0, stream>>>(n_ptr, id, g, err);
     k_grid_reorder<<<pb, T, 0, stream>>>(n_ptr, g, a, err);
     return cudaGetLastError();
+}
+
+cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
+                               float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
+                               cudaStream_t stream) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(g.count, 0, sizeof(unsigned) * static_cast<size_t>(g.ncells), stream)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
+    if ((e = grid_keys_enqueue(pos, n_ptr, cap, ox, oy, cell, dimx, dimy, g, stream)) != cudaSuccess) return e;
+    return grid_sort_enqueue(id, n_ptr, cap, g, a, err, stream);
 }
 
 __global__ void k_set_int(int* p, int v) { *p = v; }
@@ -262,7 +273,6 @@ extern "C" tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, in
     g.off = d_cell_off;  // write the offsets straight into the caller's table
     float2* scratch = reinterpret_cast<float2*>(w + 256 + tss::grid_bufs_bytes(cap, cells));
     if (cudaMemsetAsync(w, 0, 256, st) != cudaSuccess) return TSS_CUDA_ERROR;
-    if (cudaMemsetAsync(g.count, 0, sizeof(unsigned) * (size_t)cells, st) != cudaSuccess) return TSS_CUDA_ERROR;
     tss::k_set_int<<<1, 1, 0, st>>>(n_dev, n);
     tss::ReorderArgs a{};
     a.src_pos = reinterpret_cast<const float2*>(d_pos);

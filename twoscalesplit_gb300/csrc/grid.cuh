@@ -23,7 +23,7 @@
 namespace tss {
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 32;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 struct GridBufs {
@@ -64,11 +64,32 @@ __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __r
                                unsigned* err);
 __global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err);
 
-// Enqueue a whole build: clears the tile sums, then keys, scan, scatter, reorder.
-// `n_ptr` is a device int <= cap; inconsistent offsets set kErrTimeout in *err.
+// Enqueue a whole build: clears the counts and tile sums, then keys, scan,
+// scatter, reorder.  `n_ptr` is a device int <= cap; inconsistent offsets set
+// kErrTimeout in *err.
 cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
                                float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
                                cudaStream_t stream);
+// The key pass alone (counts and tile sums must be zero), and the rest of a build
+// (scan, clearing the tile sums for the next key pass, scatter, reorder).  The
+// solver's step runs the key pass inside its force kernels (grid_key below) and
+// only the rest here.
+cudaError_t grid_keys_enqueue(const float2* pos, const int* n_ptr, int cap, float ox, float oy, float cell, int dimx,
+                              int dimy, GridBufs g, cudaStream_t stream);
+cudaError_t grid_sort_enqueue(const int32_t* id, const int* n_ptr, int cap, GridBufs g, ReorderArgs a,
+                              unsigned* err, cudaStream_t stream);
+
+// The key of list entry i for the next build: its cell, its rank among the cell's
+// entries (atomic order; the reorder fixes the order by id) and the tile sum.
+// Lanes of a warp that hit the same tile add once.
+__device__ __forceinline__ void grid_key(unsigned* __restrict__ count, int* __restrict__ key, int* __restrict__ rank,
+                                         unsigned* __restrict__ tile_sum, int i, int c) {
+    key[i] = c;
+    rank[i] = static_cast<int>(atomicAdd(&count[c], 1u));
+    const unsigned t = static_cast<unsigned>(c) / kScanTile;
+    const unsigned peers = __match_any_sync(__activemask(), t);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&tile_sum[t], static_cast<unsigned>(__popc(peers)));
+}
 
 size_t grid_bufs_bytes(int cap, int ncells);
 GridBufs grid_bufs_carve(void* base, int cap, int ncells);

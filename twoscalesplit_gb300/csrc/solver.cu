@@ -110,6 +110,10 @@ struct tss_solver {
             s.nid = b.nid;
             s.ndens = b.ndens;
             s.npres = b.npres;
+            s.gcount = b.g.count;
+            s.gkey = b.g.key;
+            s.grank = b.g.rank;
+            s.gtile = b.g.tile_sum;
             return s;
         };
         v.L = sv(L);
@@ -162,12 +166,12 @@ struct tss_solver {
         cudaError_t e;
         const StepView V = view();
         if ((e = mark(0, s)) != cudaSuccess) return e;
-        // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid)
-        e = grid_build_enqueue(H.npos, H.nid, &cnt->cur[1], capH, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], H.g,
-                               reorder_args(H, true), &cnt->err, s);
+        // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid);
+        //    their key pass ran at the end of the previous step (force kernels, split)
+        //    or in prime_keys() after the state was set
+        e = grid_sort_enqueue(H.nid, &cnt->cur[1], capH, H.g, reorder_args(H, true), &cnt->err, s);
         if (e != cudaSuccess || (e = mark(1, s)) != cudaSuccess) return e;
-        e = grid_build_enqueue(L.npos, L.nid, &cnt->cur[0], nL, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], L.g,
-                               reorder_args(L, false), &cnt->err, s);
+        e = grid_sort_enqueue(L.nid, &cnt->cur[0], nL, L.g, reorder_args(L, false), &cnt->err, s);
         if (e != cudaSuccess || (e = mark(2, s)) != cudaSuccess) return e;
         // 2. relaxation of last step's children (older snapshot's relaxTransient)
         for (int it = 0; it < P.relax_iters; ++it) {
@@ -190,6 +194,20 @@ struct tss_solver {
         k_step_finish<<<1, 32, 0, s>>>(cnt);
         if ((e = mark(8, s)) != cudaSuccess) return e;
         return cudaGetLastError();
+    }
+
+    // Key pass of both grids for the current list arrays (after create or upload).
+    cudaError_t prime_keys(cudaStream_t s) {
+        cudaError_t e;
+        for (ScaleBufs* b : {&L, &H}) {
+            if ((e = cudaMemsetAsync(b->g.count, 0, sizeof(unsigned) * static_cast<size_t>(b->g.ncells), s)) !=
+                cudaSuccess)
+                return e;
+            if ((e = cudaMemsetAsync(b->g.tile_sum, 0, sizeof(unsigned) * b->g.ntiles, s)) != cudaSuccess) return e;
+        }
+        e = grid_keys_enqueue(H.npos, &cnt->cur[1], capH, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], H.g, s);
+        if (e != cudaSuccess) return e;
+        return grid_keys_enqueue(L.npos, &cnt->cur[0], nL, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], L.g, s);
     }
 
     void drop_graph() {
@@ -449,6 +467,7 @@ tss_status tss_solver_create(const tss_config* cfg, int n_low, const float* low_
     } else if (e == cudaSuccess) {
         // no walls: offsets all zero (already zeroed)
     }
+    if (e == cudaSuccess) e = s->prime_keys(st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
@@ -606,7 +625,8 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
             int nL = scale == 0 ? n : c.cur[0];
             int nH = scale == 1 ? n : c.cur[1];
             k_set_counts<<<1, 1, 0, s->stream>>>(s->cnt, nL, nH);
-            e = cudaStreamSynchronize(s->stream);
+            e = s->prime_keys(s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         }
     }
     if (e != cudaSuccess) return s->cuda_fail(e, "upload");

@@ -17,44 +17,40 @@ __device__ __forceinline__ int tid() { return blockIdx.x * blockDim.x + threadId
 __device__ __forceinline__ float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 }  // namespace
 
-// All gather kernels loop over particles in warp-uniform strides (every lane of a
-// warp makes the same number of trips, lanes past n are inactive) because gather()
-// and the split ballot are warp-synchronous.
-
 // ---------------------------------------------------------------------------
 // High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kGatherThreads) k_density_high(Params P, StepView V) {
-    __shared__ int s_list[kGatherK * kGatherThreads];
-    int* col = s_list + threadIdx.x;
+__global__ void __launch_bounds__(256) k_density_high(Params P, StepView V) {
     const int n = V.cnt->cur[1];
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool act = i < n;
-        const float2 p = act ? H.pos[i] : make_float2(0.f, 0.f);
-        const unsigned s = act ? H.st[i] : 0u;
+    for (int i = tid(); i < n; i += nthreads()) {
+        const float2 p = H.pos[i];
+        const unsigned s = H.st[i];
         float d = 0.0f, dl = 0.0f;
-        int csx = 0, csy = 0, cex = 0, cey = 0;
+        int csx, csy, cex, cey;
         grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
         grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
         {
-            Window w = act ? Window(H.off, P.dimH[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) { return lamHH(s, H.st[k]) && sq(sub(p, H.pos[k])) <= P.Tle_rh; },
-                [&](int j) {
-                    const float dist = sqrtf(sq(sub(p, H.pos[j])));
-                    d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamHH(s, H.st[k])) return false;
+                    x = sq(sub(p, H.pos[k]));
+                    return x <= P.Tle_rh;
                 });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            }
         }
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
         if (P.q1) {
             // The reference reads the HIGH sorted list at LOW-grid ranges; past
             // n_high that list still holds its initial identity (slot t at t).
-            for (int cy = csy; act && cy <= cey; ++cy) {
+            for (int cy = csy; cy <= cey; ++cy) {
                 const int row = cy * P.dimL[0];
                 const int b = L.off[row + cex + 1];
                 for (int t = L.off[row + csx]; t < b; ++t) {
@@ -79,78 +75,82 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_high(Params P, StepV
                 }
             }
         } else {
-            Window w = act ? Window(L.off, P.dimL[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) { return lamHL(s, L.st[k]) && sq(sub(p, L.pos[k])) <= P.Tle_rh; },
-                [&](int j) {
-                    const float dist = sqrtf(sq(sub(p, L.pos[j])));
-                    dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamHL(s, L.st[k])) return false;
+                    x = sq(sub(p, L.pos[k]));
+                    return x <= P.Tle_rh;
                 });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            }
         }
-        if (act) {
-            d *= P.mH;
-            dl *= P.mL;
-            d += dl;
-            const float pr = tait(d, P);
-            H.dens[i] = d;
-            H.pres[i] = pr;
-            H.q[i] = pr / (d * d);
-            if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
-        }
+        d *= P.mH;
+        dl *= P.mL;
+        d += dl;
+        const float pr = tait(d, P);
+        H.dens[i] = d;
+        H.pres[i] = pr;
+        H.q[i] = pr / (d * d);
+        if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
     }
 }
 
 // ---------------------------------------------------------------------------
 // Low-res density + Tait, computeParticleDensityPressure (WCSPHSolver.cu:1342-1424)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kGatherThreads) k_density_low(Params P, StepView V) {
-    __shared__ int s_list[kGatherK * kGatherThreads];
-    int* col = s_list + threadIdx.x;
+__global__ void __launch_bounds__(256) k_density_low(Params P, StepView V) {
     const int n = V.cnt->cur[0];
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     const bool cross = V.cnt->h_state0 != 0;  // only state-0 high-res particles can contribute
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool act = i < n;
-        const float2 p = act ? L.pos[i] : make_float2(0.f, 0.f);
-        const unsigned s = act ? L.st[i] : 0u;
+    for (int i = tid(); i < n; i += nthreads()) {
+        const float2 p = L.pos[i];
+        const unsigned s = L.st[i];
         float d = 0.0f, dh = 0.0f;
-        int csx = 0, csy = 0, cex = 0, cey = 0;
+        int csx, csy, cex, cey;
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
         {
-            Window w = act ? Window(L.off, P.dimL[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col, [&](int k) { return sq(sub(p, L.pos[k])) <= P.Tle_r; },
-                [&](int j) {
-                    const float dist = sqrtf(sq(sub(p, L.pos[j])));
-                    d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    x = sq(sub(p, L.pos[k]));
+                    return x <= P.Tle_r;
                 });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            }
         }
         if (cross) {
             grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
             grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-            Window w = act ? Window(H.off, P.dimH[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) { return lamLH(s, H.st[k]) && sq(sub(p, H.pos[k])) <= P.Tle_r; },
-                [&](int j) {
-                    const float dist = sqrtf(sq(sub(p, H.pos[j])));
-                    dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    if (!lamLH(s, H.st[k])) return false;
+                    x = sq(sub(p, H.pos[k]));
+                    return x <= P.Tle_r;
                 });
+                if (j < 0) break;
+                const float dist = sqrtf(x);
+                dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            }
         }
-        if (act) {
-            d *= P.mL;
-            dh *= P.mH;
-            const float rho = d + dh;
-            const float pr = tait(rho, P);
-            L.dens[i] = rho;
-            L.pres[i] = pr;
-            L.q[i] = pr / (rho * rho);
-            if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
-        }
+        d *= P.mL;
+        dh *= P.mH;
+        const float rho = d + dh;
+        const float pr = tait(rho, P);
+        L.dens[i] = rho;
+        L.pres[i] = pr;
+        L.q[i] = pr / (rho * rho);
+        if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
     }
 }
 
@@ -182,9 +182,7 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
 // accumulators, so they are taken in two passes over the window.  Each warp adds
 // its split count to the tile counter the compaction reads.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kGatherThreads) k_force_low(Params P, StepView V) {
-    __shared__ int s_list[kGatherK * kGatherThreads];
-    int* col = s_list + threadIdx.x;
+__global__ void __launch_bounds__(256, 6) k_force_low(Params P, StepView V) {
     const int n = V.cnt->cur[0];
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
@@ -192,49 +190,47 @@ __global__ void __launch_bounds__(kGatherThreads) k_force_low(Params P, StepView
     const int lane = threadIdx.x & 31;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int i = base + threadIdx.x;
-        const bool act = i < n;
-        float2 p = act ? L.pos[i] : make_float2(0.f, 0.f);
-        float2 v = act ? L.vel[i] : make_float2(0.f, 0.f);
-        const unsigned s = act ? L.st[i] : 0u;
-        const float dens = act ? L.dens[i] : 0.0f, qi = act ? L.q[i] : 0.0f;
-        float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
-        int csx = 0, csy = 0, cex = 0, cey = 0;
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        {
-            Window w = act ? Window(L.off, P.dimL[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) {
-                    const float x = sq(sub(p, L.pos[k]));
-                    return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
-                },
-                [&](int j) {
-                    const float2 pij = sub(p, L.pos[j]);
-                    pair_force(P, pij, sqrtf(sq(pij)), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc,
-                               accT);
-                });
-        }
-        const float2 accB = act ? wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL) : make_float2(0.f, 0.f);
-        if (cross) {
-            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-            Window w = act ? Window(H.off, P.dimH[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) {
-                    if (!lamLH(s, H.st[k])) return false;
-                    const float x = sq(sub(p, H.pos[k]));
-                    return x != 0.0f && x <= P.Tlt_r;
-                },
-                [&](int j) {
-                    const float2 pij = sub(p, H.pos[j]);
-                    pair_force(P, pij, sqrtf(sq(pij)), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH,
-                               accT);
-                });
-        }
         bool flag = false;
-        if (act) {
+        if (i < n) {
+            float2 p = L.pos[i], v = L.vel[i];
+            const unsigned s = L.st[i];
+            const float dens = L.dens[i], qi = L.q[i];
+            float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
+            int csx, csy, cex, cey;
+            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+            {
+                Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+                float2 pij = make_float2(0.f, 0.f);
+                float x = 0.0f;
+                for (;;) {
+                    const int j = w.next([&](int k) {
+                        pij = sub(p, L.pos[k]);
+                        x = sq(pij);
+                        return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
+                    });
+                    if (j < 0) break;
+                    pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
+                }
+            }
+            const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
+            if (cross) {
+                grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+                grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+                Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+                float2 pij = make_float2(0.f, 0.f);
+                float x = 0.0f;
+                for (;;) {
+                    const int j = w.next([&](int k) {
+                        if (!lamLH(s, H.st[k])) return false;
+                        pij = sub(p, H.pos[k]);
+                        x = sq(pij);
+                        return x != 0.0f && x <= P.Tlt_r;
+                    });
+                    if (j < 0) break;
+                    pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
+                }
+            }
             acc.x *= -P.mL;
             acc.y *= -P.mL;
             accH.x *= -P.mH;
@@ -255,6 +251,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_force_low(Params P, StepView
             L.npos[i] = p;
             L.nvel[i] = v;
             L.nid[i] = L.id[i];
+            grid_key(L.gcount, L.gkey, L.grank, L.gtile, i, cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
             uint8_t ns = static_cast<uint8_t>(s);
             if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
                 ns = 1;
@@ -359,6 +356,8 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
                         V.H.nvel[h] = v;
                         V.H.nst[h] = 1;
                         V.H.nid[h] = 4 * id + c;
+                        grid_key(V.H.gcount, V.H.gkey, V.H.grank, V.H.gtile, h,
+                                 cell_hash(cp[c], P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
                         if (V.H.ndens) {
                             V.H.ndens[h] = 0.0f;
                             V.H.npres[h] = 0.0f;
@@ -377,57 +376,51 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
 // Reads see the pre-step state (the reference integrates in place, a data race);
 // low-res states are read after this step's split marks, as in the reference.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kGatherThreads) k_force_high(Params P, StepView V) {
-    __shared__ int s_list[kGatherK * kGatherThreads];
-    int* col = s_list + threadIdx.x;
+__global__ void __launch_bounds__(256, 6) k_force_high(Params P, StepView V) {
     const int n = V.cnt->cur[1];
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool act = i < n;
-        float2 p = act ? H.pos[i] : make_float2(0.f, 0.f);
-        float2 v = act ? H.vel[i] : make_float2(0.f, 0.f);
-        const unsigned s = act ? H.st[i] : 0u;
-        const float dens = act ? H.dens[i] : 0.0f, qi = act ? H.q[i] : 0.0f;
+    for (int i = tid(); i < n; i += nthreads()) {
+        float2 p = H.pos[i], v = H.vel[i];
+        const unsigned s = H.st[i];
+        const float dens = H.dens[i], qi = H.q[i];
         float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
-        int csx = 0, csy = 0, cex = 0, cey = 0;
+        int csx, csy, cex, cey;
         grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
         grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
         {
-            Window w = act ? Window(H.off, P.dimH[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) {
+            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
+            float2 pij = make_float2(0.f, 0.f);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
                     if (!lamHH(s, H.st[k])) return false;
-                    const float x = sq(sub(p, H.pos[k]));
+                    pij = sub(p, H.pos[k]);
+                    x = sq(pij);
                     return x != 0.0f && x <= P.Tlt_rh;
-                },
-                [&](int j) {
-                    const float2 pij = sub(p, H.pos[j]);
-                    pair_force(P, pij, sqrtf(sq(pij)), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc,
-                               accT);
                 });
+                if (j < 0) break;
+                pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
+            }
         }
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
         {
-            Window w = act ? Window(L.off, P.dimL[0], csx, cex, csy, cey) : Window();
-            gather(
-                w, act, col,
-                [&](int k) {
-                    const unsigned sj = L.nst[k];  // low-res states after this step's split marks
+            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
+            float2 pij = make_float2(0.f, 0.f);
+            float x = 0.0f;
+            for (;;) {
+                const int j = w.next([&](int k) {
+                    const unsigned sj = L.nst[k];
                     if (!(lamHL(s, sj) && notDeleted(sj))) return false;
-                    const float x = sq(sub(p, L.pos[k]));
+                    pij = sub(p, L.pos[k]);
+                    x = sq(pij);
                     return x != 0.0f && x <= P.Tlt_r;
-                },
-                [&](int j) {
-                    const float2 pij = sub(p, L.pos[j]);
-                    pair_force(P, pij, sqrtf(sq(pij)), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL,
-                               accT);
                 });
+                if (j < 0) break;
+                pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
+            }
         }
-        if (!act) continue;  // warp-uniform work is done; the rest is per particle
         const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
         acc.x *= -P.mH;
         acc.y *= -P.mH;
@@ -467,6 +460,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_force_high(Params P, StepVie
         H.nvel[i] = v;
         H.nst[i] = static_cast<uint8_t>(s);
         H.nid[i] = id;
+        grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, cell_hash(p, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
         if (H.ndens) {
             H.ndens[i] = dens;
             H.npres[i] = H.pres[i];

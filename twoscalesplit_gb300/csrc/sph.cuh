@@ -1,5 +1,6 @@
 // sph.cuh -- the gather kernels of one two-scale WCSPH step.
 #pragma once
+#include "grid.cuh"
 #include "tss_device.cuh"
 
 namespace tss {
@@ -24,6 +25,11 @@ struct ScaleView {
     int32_t* nid;
     float* ndens;    // carried densities/pressures (relaxation only; may be null)
     float* npres;
+    // the next step's grid keys, written where the list entries are written
+    unsigned* gcount;
+    int* gkey;
+    int* grank;
+    unsigned* gtile;
 };
 
 struct StepView {

@@ -173,35 +173,6 @@ struct Window {
 
 __device__ __forceinline__ float sq(float2 v) { return v.x * v.x + v.y * v.y; }
 
-// Two-phase, warp-synchronous gather.  Phase 1: each lane walks its window and
-// writes the indices of up to kGatherK accepted candidates, in order, to its column
-// of a shared-memory list.  Phase 2: the warp runs `pair` for list entry 0, 1, ...
-// up to the longest lane's count, every lane on its own entry, so the expensive
-// pair arithmetic runs with (nearly) all lanes active; per lane the pairs are still
-// taken in window order, so every sum is the reference's.  Repeats until every
-// lane's window is exhausted.  All 32 lanes of the warp must call it (inactive
-// lanes pass active = false and an empty Window).
-constexpr int kGatherThreads = 256;
-constexpr int kGatherK = 16;
 
-template <class Accept, class Pair>
-__device__ __forceinline__ void gather(Window& w, bool active, int* col, Accept&& accept, Pair&& pair) {
-    bool more = active;
-    while (__any_sync(0xffffffffu, more)) {
-        int cnt = 0;
-        while (more && cnt < kGatherK) {
-            const int j = w.next(accept);
-            if (j < 0) {
-                more = false;
-            } else {
-                col[cnt * kGatherThreads] = j;
-                ++cnt;
-            }
-        }
-        const int maxc = __reduce_max_sync(0xffffffffu, cnt);
-        for (int k = 0; k < maxc; ++k)
-            if (k < cnt) pair(col[k * kGatherThreads]);
-    }
-}
 
 }  // namespace tss

@@ -95,6 +95,39 @@ tss_status tss_solver_create(const tss_config* cfg,
                              tss_solver** out);
 void tss_solver_destroy(tss_solver* s);
 
+/* ------------------------------------------------------------------------- */
+/* Batches: many independent scenes advanced by the same kernel launches        */
+/* ------------------------------------------------------------------------- */
+/* One scene of a batch: its own configuration (domain, radii, constants, ROI,
+ * dt; relax_iters must be equal across a batch), particles and walls. */
+typedef struct tss_scene_desc {
+    const tss_config* config;
+    int n_low;
+    const float* low_pos;      /* host, 2*n_low floats  */
+    const float* low_vel;      /* may be NULL           */
+    float mass_low;
+    float mass_high;
+    int n_wall;
+    const float* wall_pos;     /* host, 2*n_wall floats */
+    float mass_wall;
+} tss_scene_desc;
+
+/* Create a batch of n_scenes scenes sharing one high-res pool of cap_high
+ * particles.  The scenes' grids are laid side by side in one global cell space,
+ * so one grid build and one launch of each kernel advance all of them; a scene's
+ * results are the same as when it runs alone (the reference's solver held one
+ * scene per process, WCSPHSolver.cu:2728).  The returned handle works with every
+ * tss_solver_* call; slot ids are global (scene k's low-res particle i is
+ * sum_{j<k} n_low_j + i); tss_solver_download_scene returns one scene with its
+ * own ids. */
+tss_status tss_batch_create(int n_scenes, const tss_scene_desc* scenes, int cap_high, tss_solver** out);
+tss_status tss_solver_num_scenes(tss_solver* s, int* n_scenes);
+/* Per-scene particle counts (arrays of n_scenes ints, either may be NULL). */
+tss_status tss_solver_scene_counts(tss_solver* s, int* n_low, int* n_high);
+/* One scene's state, scene-local ids (low: 0..n_low-1, high: 4*low id + child). */
+struct tss_scale_state;
+tss_status tss_solver_download_scene(tss_solver* s, int scene, int scale, struct tss_scale_state* out);
+
 /* Advance n_steps steps (WCSPHSolver::AdvanceTS, WCSPHSolver.cu:2726-2810), enqueued
  * on `stream` (a cudaStream_t; NULL = the default stream, as the reference used).
  * Nothing is copied back to the host; the particle counts stay on the device.  The

@@ -7,9 +7,9 @@ solver interface, the scene generators and the build script.
 from ._abi import (TSS_FLAG_Q1_COMPAT, TSS_SCALE_HIGH, TSS_SCALE_LOW, TssConfig, TssError, config_init,
                    load_library)
 from .scenes import Scene, make_scene
-from .solver import (CreateParticleBox, CreateParticleBoxCanvas, ParticleSystem, Solver, WCSPHConfig,
+from .solver import (Batch, CreateParticleBox, CreateParticleBoxCanvas, ParticleSystem, Solver, WCSPHConfig,
                      WCSPHSolver)
 
 __all__ = ["TSS_FLAG_Q1_COMPAT", "TSS_SCALE_HIGH", "TSS_SCALE_LOW", "TssConfig", "TssError", "config_init",
            "load_library", "Scene", "make_scene", "CreateParticleBox", "CreateParticleBoxCanvas", "ParticleSystem",
-           "Solver", "WCSPHConfig", "WCSPHSolver"]
+           "Solver", "Batch", "WCSPHConfig", "WCSPHSolver"]

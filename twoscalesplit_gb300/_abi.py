@@ -94,6 +94,13 @@ class TssScaleState(ctypes.Structure):
                 ("pres", ctypes.POINTER(ctypes.c_float))]
 
 
+class TssSceneDesc(ctypes.Structure):
+    _fields_ = [("config", ctypes.POINTER(TssConfig)), ("n_low", ctypes.c_int),
+                ("low_pos", ctypes.POINTER(ctypes.c_float)), ("low_vel", ctypes.POINTER(ctypes.c_float)),
+                ("mass_low", ctypes.c_float), ("mass_high", ctypes.c_float), ("n_wall", ctypes.c_int),
+                ("wall_pos", ctypes.POINTER(ctypes.c_float)), ("mass_wall", ctypes.c_float)]
+
+
 class TssBuffers(ctypes.Structure):
     _fields_ = [("pos", ctypes.c_void_p * 2), ("vel", ctypes.c_void_p * 2), ("dens", ctypes.c_void_p * 2),
                 ("id", ctypes.c_void_p * 2), ("state", ctypes.c_void_p * 2), ("counts", ctypes.c_void_p)]
@@ -166,6 +173,10 @@ def load_library(path=None):
         "tss_solver_stage_times": (i, [vp, fp, i]),
         "tss_status_string": (ctypes.c_char_p, [i]),
         "tss_grid_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
+        "tss_batch_create": (i, [i, ctypes.POINTER(TssSceneDesc), i, ctypes.POINTER(vp)]),
+        "tss_solver_num_scenes": (i, [vp, ctypes.POINTER(i)]),
+        "tss_solver_scene_counts": (i, [vp, ip, ip]),
+        "tss_solver_download_scene": (i, [vp, i, i, ctypes.POINTER(TssScaleState)]),
         "tss_grid_build": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp, ctypes.c_size_t, vp]),
         "tss_grid_build_noalloc": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp]),
     }

@@ -166,6 +166,7 @@ __global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, Reorde
             a.dst_pres[dst] = a.src_pres[src];
         }
         if (a.dst_order) a.dst_order[dst] = src;
+        if (a.dst_sc) a.dst_sc[dst] = static_cast<uint16_t>(scene_of_slot(a.slot_base, a.nscenes, id >> a.id_shift));
         if (a.slot_map) {
             if (id >= 0 && id < a.slots) a.slot_map[id] = dst;
             else atomicOr(err, kErrTimeout);

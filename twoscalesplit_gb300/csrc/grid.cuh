@@ -53,6 +53,12 @@ struct ReorderArgs {
     int32_t* dst_order;        // may be null: source list index of each sorted position
     int32_t* slot_map;         // may be null: slot id -> sorted index
     int slots;                 // size of slot_map
+    // batches: the scene of each sorted entry, found from its slot id
+    // (slot_base[s] <= id >> id_shift < slot_base[s + 1])
+    uint16_t* dst_sc;          // may be null
+    const int* slot_base;      // [nscenes + 1], ascending
+    int nscenes;
+    int id_shift;              // 0 for low-res ids, 2 for high-res (4 children per parent)
     int* h_state0;             // may be null: set to 1 if some entry has (state & 1) == 0
 };
 
@@ -60,6 +66,17 @@ __global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restric
                             float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
                             int* __restrict__ rank, unsigned* __restrict__ tile_sum);
 __global__ void k_grid_scan(GridBufs g);
+// Scene of a slot id: the s with slot_base[s] <= low_slot < slot_base[s + 1].
+__device__ __forceinline__ int scene_of_slot(const int* __restrict__ slot_base, int nscenes, int low_slot) {
+    int lo = 0, hi = nscenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (slot_base[mid] <= low_slot) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
                                unsigned* err);
 __global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err);

@@ -7,6 +7,11 @@
 // L1.  Each thread sums its candidates in the reference's order (cells row by row,
 // particles in cell order), which keeps every FP32 sum identical to the reference's
 // for the same list order.
+//
+// Each kernel's per-particle work is an inlined function of the particle's Params:
+// the kernel's own constants for a single scene, the scene's table row for a
+// batch.  A scene's cell windows index its grid at its cell base in the global
+// cell space, so one sort and one offset table serve all scenes of a batch.
 #include "sph.cuh"
 
 namespace tss {
@@ -17,140 +22,168 @@ __device__ __forceinline__ int tid() { return blockIdx.x * blockDim.x + threadId
 __device__ __forceinline__ float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 }  // namespace
 
+
 // ---------------------------------------------------------------------------
 // High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_density_high(Params P, StepView V) {
-    const int n = V.cnt->cur[1];
+__device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
-    for (int i = tid(); i < n; i += nthreads()) {
-        const float2 p = H.pos[i];
-        const unsigned s = H.st[i];
-        float d = 0.0f, dl = 0.0f;
-        int csx, csy, cex, cey;
-        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        {
-            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
-            float x = 0.0f;
-            for (;;) {
-                const int j = w.next([&](int k) {
-                    if (!lamHH(s, H.st[k])) return false;
-                    x = sq(sub(p, H.pos[k]));
-                    return x <= P.Tle_rh;
-                });
-                if (j < 0) break;
-                const float dist = sqrtf(x);
-                d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
-            }
+    const int* offH = H.off + P.cbH;
+    const int* offL = L.off + P.cbL;
+    const float2 p = H.pos[i];
+    const unsigned s = H.st[i];
+    float d = 0.0f, dl = 0.0f;
+    int csx, csy, cex, cey;
+    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    {
+        Window w(offH, P.dimH[0], csx, cex, csy, cey);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                if (!lamHH(s, H.st[k])) return false;
+                x = sq(sub(p, H.pos[k]));
+                return x <= P.Tle_rh;
+            });
+            if (j < 0) break;
+            const float dist = sqrtf(x);
+            d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
         }
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        if (P.q1) {
-            // The reference reads the HIGH sorted list at LOW-grid ranges; past
-            // n_high that list still holds its initial identity (slot t at t).
-            for (int cy = csy; cy <= cey; ++cy) {
-                const int row = cy * P.dimL[0];
-                const int b = L.off[row + cex + 1];
-                for (int t = L.off[row + csx]; t < b; ++t) {
-                    float2 pj = make_float2(0.0f, 0.0f);
-                    unsigned sj = 0;
-                    if (t < n) {
-                        pj = H.pos[t];
-                        sj = H.st[t];
-                    } else {
-                        int k = t < P.slotsH ? H.map[t] : -1;
-                        if (k >= 0) {
-                            pj = H.pos[k];
-                            sj = H.st[k];
-                        }
-                    }
-                    if (!lamHL(s, sj)) continue;
-                    const float x = sq(sub(p, pj));
-                    if (x <= P.Tle_rh) {
-                        const float dist = sqrtf(x);
-                        d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+    }
+    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    if (P.q1) {
+        // The reference reads the HIGH sorted list at LOW-grid ranges of its own
+        // scene; past the scene's n_high that list still holds its initial identity
+        // (slot t at position t).
+        const int baseL = offL[0], baseH = offH[0];
+        const int nHs = offH[P.CHs] - baseH;
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * P.dimL[0];
+            const int b = offL[row + cex + 1];
+            for (int t = offL[row + csx]; t < b; ++t) {
+                const int tl = t - baseL;
+                float2 pj = make_float2(0.0f, 0.0f);
+                unsigned sj = 0;
+                if (tl < nHs) {
+                    pj = H.pos[baseH + tl];
+                    sj = H.st[baseH + tl];
+                } else {
+                    const int slot = 4 * P.sbL + tl;
+                    const int k = (tl < 4 * P.nLs && slot < P.slotsH) ? H.map[slot] : -1;
+                    if (k >= 0) {
+                        pj = H.pos[k];
+                        sj = H.st[k];
                     }
                 }
-            }
-        } else {
-            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
-            float x = 0.0f;
-            for (;;) {
-                const int j = w.next([&](int k) {
-                    if (!lamHL(s, L.st[k])) return false;
-                    x = sq(sub(p, L.pos[k]));
-                    return x <= P.Tle_rh;
-                });
-                if (j < 0) break;
-                const float dist = sqrtf(x);
-                dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                if (!lamHL(s, sj)) continue;
+                const float x = sq(sub(p, pj));
+                if (x <= P.Tle_rh) {
+                    const float dist = sqrtf(x);
+                    d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                }
             }
         }
-        d *= P.mH;
-        dl *= P.mL;
-        d += dl;
-        const float pr = tait(d, P);
-        H.dens[i] = d;
-        H.pres[i] = pr;
-        H.q[i] = pr / (d * d);
-        if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    } else {
+        Window w(offL, P.dimL[0], csx, cex, csy, cey);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                if (!lamHL(s, L.st[k])) return false;
+                x = sq(sub(p, L.pos[k]));
+                return x <= P.Tle_rh;
+            });
+            if (j < 0) break;
+            const float dist = sqrtf(x);
+            dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+        }
+    }
+    d *= P.mH;
+    dl *= P.mL;
+    d += dl;
+    const float pr = tait(d, P);
+    H.dens[i] = d;
+    H.pres[i] = pr;
+    H.q[i] = pr / (d * d);
+    if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+}
+
+template <bool B>
+__global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
+    const int n = V.cnt->cur[1];
+    for (int i = tid(); i < n; i += nthreads()) {
+        if constexpr (B) {
+            const Params P = V.table[V.scH[i]];
+            density_high_one(P, V, i);
+        } else {
+            density_high_one(P0, V, i);
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
 // Low-res density + Tait, computeParticleDensityPressure (WCSPHSolver.cu:1342-1424)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_density_low(Params P, StepView V) {
-    const int n = V.cnt->cur[0];
+__device__ __forceinline__ void density_low_one(const Params& P, const StepView& V, int i, bool cross) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
-    const bool cross = V.cnt->h_state0 != 0;  // only state-0 high-res particles can contribute
+    const float2 p = L.pos[i];
+    const unsigned s = L.st[i];
+    float d = 0.0f, dh = 0.0f;
+    int csx, csy, cex, cey;
+    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    {
+        Window w(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                x = sq(sub(p, L.pos[k]));
+                return x <= P.Tle_r;
+            });
+            if (j < 0) break;
+            const float dist = sqrtf(x);
+            d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+        }
+    }
+    if (cross) {  // only state-0 high-res particles can contribute (lambda_LH)
+        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        Window w(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                if (!lamLH(s, H.st[k])) return false;
+                x = sq(sub(p, H.pos[k]));
+                return x <= P.Tle_r;
+            });
+            if (j < 0) break;
+            const float dist = sqrtf(x);
+            dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+        }
+    }
+    d *= P.mL;
+    dh *= P.mH;
+    const float rho = d + dh;
+    const float pr = tait(rho, P);
+    L.dens[i] = rho;
+    L.pres[i] = pr;
+    L.q[i] = pr / (rho * rho);
+    if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+}
+
+template <bool B>
+__global__ void __launch_bounds__(256) k_density_low(Params P0, StepView V) {
+    const int n = V.cnt->cur[0];
+    const bool cross = V.cnt->h_state0 != 0;
     for (int i = tid(); i < n; i += nthreads()) {
-        const float2 p = L.pos[i];
-        const unsigned s = L.st[i];
-        float d = 0.0f, dh = 0.0f;
-        int csx, csy, cex, cey;
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        {
-            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
-            float x = 0.0f;
-            for (;;) {
-                const int j = w.next([&](int k) {
-                    x = sq(sub(p, L.pos[k]));
-                    return x <= P.Tle_r;
-                });
-                if (j < 0) break;
-                const float dist = sqrtf(x);
-                d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
-            }
+        if constexpr (B) {
+            const Params P = V.table[V.scL[i]];
+            density_low_one(P, V, i, cross);
+        } else {
+            density_low_one(P0, V, i, cross);
         }
-        if (cross) {
-            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
-            float x = 0.0f;
-            for (;;) {
-                const int j = w.next([&](int k) {
-                    if (!lamLH(s, H.st[k])) return false;
-                    x = sq(sub(p, H.pos[k]));
-                    return x <= P.Tle_r;
-                });
-                if (j < 0) break;
-                const float dist = sqrtf(x);
-                dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
-            }
-        }
-        d *= P.mL;
-        dh *= P.mH;
-        const float rho = d + dh;
-        const float pr = tait(rho, P);
-        L.dens[i] = rho;
-        L.pres[i] = pr;
-        L.q[i] = pr / (rho * rho);
-        if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
     }
 }
 
@@ -160,10 +193,11 @@ __global__ void __launch_bounds__(256) k_density_low(Params P, StepView V) {
 __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, float2 p, int csx, int cex, int csy,
                                            int cey, float rad, float Tle, float cB) {
     float2 accB = make_float2(0.f, 0.f);
+    const int* woff = V.woff + P.cbL;
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimL[0];
-        const int wb = V.woff[row + cex + 1];
-        for (int k = V.woff[row + csx]; k < wb; ++k) {
+        const int wb = woff[row + cex + 1];
+        for (int k = woff[row + csx]; k < wb; ++k) {
             const float2 pik = sub(p, V.wpos[k]);
             const float x = sq(pik);
             if (x > Tle) continue;  // NaN passes: the reference's 0 * NaN offset propagates it
@@ -179,92 +213,107 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
 // Low-res force + advance + split test: computeParticleAcceleration
 // (WCSPHSolver.cu:1648-1865) with advance (1604-1646) fused; its predicted position
 // is the advanced position bit for bit.  The fluid and wall sums are independent
-// accumulators, so they are taken in two passes over the window.  Each warp adds
-// its split count to the tile counter the compaction reads.
+// accumulators, so they are taken in two passes over the window.  The new position
+// also gives the entry's key for the next step's grid.  Returns the split flag.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 6) k_force_low(Params P, StepView V) {
-    const int n = V.cnt->cur[0];
+__device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V, int i, bool cross) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
+    float2 p = L.pos[i], v = L.vel[i];
+    const unsigned s = L.st[i];
+    const float dens = L.dens[i], qi = L.q[i];
+    float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
+    int csx, csy, cex, cey;
+    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    {
+        Window w(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey);
+        float2 pij = make_float2(0.f, 0.f);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                pij = sub(p, L.pos[k]);
+                x = sq(pij);
+                return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
+            });
+            if (j < 0) break;
+            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
+        }
+    }
+    const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
+    if (cross) {
+        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        Window w(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey);
+        float2 pij = make_float2(0.f, 0.f);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                if (!lamLH(s, H.st[k])) return false;
+                pij = sub(p, H.pos[k]);
+                x = sq(pij);
+                return x != 0.0f && x <= P.Tlt_r;
+            });
+            if (j < 0) break;
+            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
+        }
+    }
+    acc.x *= -P.mL;
+    acc.y *= -P.mL;
+    accH.x *= -P.mH;
+    accH.y *= -P.mH;
+    acc.x += accH.x;
+    acc.y += accH.y;
+    acc.x -= P.sigma * accT.x;
+    acc.y -= P.sigma * accT.y;
+    acc.x += accB.x;
+    acc.y += accB.y;
+    acc.y -= P.g;
+    L.acc[i] = acc;
+    if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+    v.x += P.dt * acc.x;
+    v.y += P.dt * acc.y;
+    p.x += P.dt * v.x;
+    p.y += P.dt * v.y;
+    L.npos[i] = p;
+    L.nvel[i] = v;
+    L.nid[i] = L.id[i];
+    grid_key(L.gcount, L.gkey, L.grank, L.gtile, i,
+             P.cbL + cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
+    bool flag = false;
+    uint8_t ns = static_cast<uint8_t>(s);
+    if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
+        ns = 1;
+        flag = true;
+    }
+    L.nst[i] = ns;
+    V.split_flag[i] = flag ? 1 : 0;
+    if (L.ndens) {
+        L.ndens[i] = dens;
+        L.npres[i] = L.pres[i];
+    }
+    return flag;
+}
+
+// Warp-uniform loop: every lane makes the same number of trips (lanes past n are
+// inactive) so the ballot that feeds the split compaction sees whole warps; a
+// warp's 32 particles lie in one compaction tile (kSplitTile % 32 == 0).
+template <bool B>
+__global__ void __launch_bounds__(256, 6) k_force_low(Params P0, StepView V) {
+    const int n = V.cnt->cur[0];
     const bool cross = V.cnt->h_state0 != 0;
     const int lane = threadIdx.x & 31;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int i = base + threadIdx.x;
         bool flag = false;
         if (i < n) {
-            float2 p = L.pos[i], v = L.vel[i];
-            const unsigned s = L.st[i];
-            const float dens = L.dens[i], qi = L.q[i];
-            float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
-            int csx, csy, cex, cey;
-            grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-            grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-            {
-                Window w(L.off, P.dimL[0], csx, cex, csy, cey);
-                float2 pij = make_float2(0.f, 0.f);
-                float x = 0.0f;
-                for (;;) {
-                    const int j = w.next([&](int k) {
-                        pij = sub(p, L.pos[k]);
-                        x = sq(pij);
-                        return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
-                    });
-                    if (j < 0) break;
-                    pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
-                }
-            }
-            const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
-            if (cross) {
-                grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-                grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-                Window w(H.off, P.dimH[0], csx, cex, csy, cey);
-                float2 pij = make_float2(0.f, 0.f);
-                float x = 0.0f;
-                for (;;) {
-                    const int j = w.next([&](int k) {
-                        if (!lamLH(s, H.st[k])) return false;
-                        pij = sub(p, H.pos[k]);
-                        x = sq(pij);
-                        return x != 0.0f && x <= P.Tlt_r;
-                    });
-                    if (j < 0) break;
-                    pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
-                }
-            }
-            acc.x *= -P.mL;
-            acc.y *= -P.mL;
-            accH.x *= -P.mH;
-            accH.y *= -P.mH;
-            acc.x += accH.x;
-            acc.y += accH.y;
-            acc.x -= P.sigma * accT.x;
-            acc.y -= P.sigma * accT.y;
-            acc.x += accB.x;
-            acc.y += accB.y;
-            acc.y -= P.g;
-            L.acc[i] = acc;
-            if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
-            v.x += P.dt * acc.x;
-            v.y += P.dt * acc.y;
-            p.x += P.dt * v.x;
-            p.y += P.dt * v.y;
-            L.npos[i] = p;
-            L.nvel[i] = v;
-            L.nid[i] = L.id[i];
-            grid_key(L.gcount, L.gkey, L.grank, L.gtile, i, cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
-            uint8_t ns = static_cast<uint8_t>(s);
-            if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
-                ns = 1;
-                flag = true;
-            }
-            L.nst[i] = ns;
-            V.split_flag[i] = flag ? 1 : 0;
-            if (L.ndens) {
-                L.ndens[i] = dens;
-                L.npres[i] = L.pres[i];
+            if constexpr (B) {
+                const Params P = V.table[V.scL[i]];
+                flag = force_low_one(P, V, i, cross);
+            } else {
+                flag = force_low_one(P0, V, i, cross);
             }
         }
-        // a warp's 32 particles lie in one compaction tile (kSplitTile % 32 == 0)
         const unsigned m = __ballot_sync(0xffffffffu, flag);
         if (lane == 0 && m) atomicAdd(&V.split_tile[(base + (threadIdx.x & ~31)) / kSplitTile], __popc(m));
     }
@@ -277,13 +326,38 @@ __global__ void __launch_bounds__(256, 6) k_force_low(Params P, StepView V) {
 // WCSPHSolver.cu:956-1005): children of the k-th split parent in sorted order
 // take high-res list entries n_high + 4k + 0..3.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
+__device__ __forceinline__ void make_children(const Params& P, const StepView& V, int i, int id, long long hb) {
+    const float2 p = V.L.npos[i], v = V.L.nvel[i];
+    const float rho = V.L.dens[i];
+    const float rad =
+        static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(2.0f * rho) * kPi)));
+    const float2 cp[4] = {make_float2(p.x + rad, p.y + rad), make_float2(p.x - rad, p.y + rad),
+                          make_float2(p.x + rad, p.y - rad), make_float2(p.x - rad, p.y - rad)};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int h = static_cast<int>(hb) + c;
+        V.H.npos[h] = cp[c];
+        V.H.nvel[h] = v;
+        V.H.nst[h] = 1;
+        V.H.nid[h] = 4 * id + c;
+        grid_key(V.H.gcount, V.H.gkey, V.H.grank, V.H.gtile, h,
+                 P.cbH + cell_hash(cp[c], P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
+        if (V.H.ndens) {
+            V.H.ndens[h] = 0.0f;
+            V.H.npres[h] = 0.0f;
+        }
+    }
+}
+
+template <bool B>
+__global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) {
     __shared__ unsigned s_warp[kSplitThreads / 32];
     __shared__ unsigned s_red[kSplitThreads / 32];
     const int tile = blockIdx.x;
     const int n = V.cnt->cur[0];
     const int nH = V.cnt->cur[1];
     const int ntiles = gridDim.x;
+    const int capH = P0.capH;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned before = 0;
     for (int t = threadIdx.x; t < tile; t += blockDim.x) before += V.split_tile[t];
@@ -321,9 +395,9 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
             const int nsplit = static_cast<int>(total);
             long long want = static_cast<long long>(nH) + 4LL * nsplit;
             V.cnt->n_split = nsplit;
-            if (want > P.capH) {
+            if (want > capH) {
                 atomicOr(&V.cnt->err, kErrCapacity);
-                want = nH + 4LL * ((P.capH - nH) / 4);
+                want = nH + 4LL * ((capH - nH) / 4);
             }
             V.cnt->next[1] = static_cast<int>(want);
             V.cnt->next[0] = n;
@@ -342,26 +416,12 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
                 const int id = V.L.id[i];
                 V.split_ids[r] = id;
                 const long long hb = static_cast<long long>(nH) + 4LL * r;
-                if (hb + 4 <= P.capH) {
-                    const float2 p = V.L.npos[i], v = V.L.nvel[i];
-                    const float rho = V.L.dens[i];
-                    const float rad = static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) /
-                                                                     (static_cast<double>(2.0f * rho) * kPi)));
-                    const float2 cp[4] = {make_float2(p.x + rad, p.y + rad), make_float2(p.x - rad, p.y + rad),
-                                          make_float2(p.x + rad, p.y - rad), make_float2(p.x - rad, p.y - rad)};
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const int h = static_cast<int>(hb) + c;
-                        V.H.npos[h] = cp[c];
-                        V.H.nvel[h] = v;
-                        V.H.nst[h] = 1;
-                        V.H.nid[h] = 4 * id + c;
-                        grid_key(V.H.gcount, V.H.gkey, V.H.grank, V.H.gtile, h,
-                                 cell_hash(cp[c], P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
-                        if (V.H.ndens) {
-                            V.H.ndens[h] = 0.0f;
-                            V.H.npres[h] = 0.0f;
-                        }
+                if (hb + 4 <= capH) {
+                    if constexpr (B) {
+                        const Params P = V.table[V.scL[i]];
+                        make_children(P, V, i, id, hb);
+                    } else {
+                        make_children(P0, V, i, id, hb);
                     }
                 }
             }
@@ -376,94 +436,103 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P, StepView V) {
 // Reads see the pre-step state (the reference integrates in place, a data race);
 // low-res states are read after this step's split marks, as in the reference.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 6) k_force_high(Params P, StepView V) {
-    const int n = V.cnt->cur[1];
+__device__ __forceinline__ void force_high_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
+    float2 p = H.pos[i], v = H.vel[i];
+    const unsigned s = H.st[i];
+    const float dens = H.dens[i], qi = H.q[i];
+    float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
+    int csx, csy, cex, cey;
+    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    {
+        Window w(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey);
+        float2 pij = make_float2(0.f, 0.f);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                if (!lamHH(s, H.st[k])) return false;
+                pij = sub(p, H.pos[k]);
+                x = sq(pij);
+                return x != 0.0f && x <= P.Tlt_rh;
+            });
+            if (j < 0) break;
+            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
+        }
+    }
+    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    {
+        Window w(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey);
+        float2 pij = make_float2(0.f, 0.f);
+        float x = 0.0f;
+        for (;;) {
+            const int j = w.next([&](int k) {
+                const unsigned sj = L.nst[k];  // low-res states after this step's split marks
+                if (!(lamHL(s, sj) && notDeleted(sj))) return false;
+                pij = sub(p, L.pos[k]);
+                x = sq(pij);
+                return x != 0.0f && x <= P.Tlt_r;
+            });
+            if (j < 0) break;
+            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
+        }
+    }
+    const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
+    acc.x *= -P.mH;
+    acc.y *= -P.mH;
+    accL.x *= -P.mL;
+    accL.y *= -P.mL;
+    acc.x -= P.sigma * accT.x;
+    acc.y -= P.sigma * accT.y;
+    acc.x += accL.x;
+    acc.y += accL.y;
+    acc.x += accB.x;
+    acc.y += accB.y;
+    acc.y -= P.g;
+    H.acc[i] = acc;
+    if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+    v.x += P.dt * acc.x;
+    v.y += P.dt * acc.y;
+    p.x += P.dt * v.x;
+    p.y += P.dt * v.y;
+    // tether to the parent after the parent's advance (adjustPosition, 1007-1022)
+    const int id = H.id[i];
+    const int parent = id >> 2;
+    if (parent >= 0 && parent < P.slotsL) {
+        const int pi = L.map[parent];
+        if (pi >= 0 && L.st[pi] == 1) {
+            const float2 pl = L.npos[pi];
+            const float rho = L.dens[pi];
+            const float2 pji = sub(p, pl);
+            const float dist = vnorm(pji);
+            const float lim = static_cast<float>(fmin(
+                static_cast<double>(dist), 0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(rho) * kPi))));
+            p.x = pl.x + lim / dist * pji.x;
+            p.y = pl.y + lim / dist * pji.y;
+        }
+    }
+    H.npos[i] = p;
+    H.nvel[i] = v;
+    H.nst[i] = static_cast<uint8_t>(s);
+    H.nid[i] = id;
+    grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, P.cbH + cell_hash(p, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
+    if (H.ndens) {
+        H.ndens[i] = dens;
+        H.npres[i] = H.pres[i];
+    }
+}
+
+template <bool B>
+__global__ void __launch_bounds__(256, 6) k_force_high(Params P0, StepView V) {
+    const int n = V.cnt->cur[1];
     for (int i = tid(); i < n; i += nthreads()) {
-        float2 p = H.pos[i], v = H.vel[i];
-        const unsigned s = H.st[i];
-        const float dens = H.dens[i], qi = H.q[i];
-        float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
-        int csx, csy, cex, cey;
-        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        {
-            Window w(H.off, P.dimH[0], csx, cex, csy, cey);
-            float2 pij = make_float2(0.f, 0.f);
-            float x = 0.0f;
-            for (;;) {
-                const int j = w.next([&](int k) {
-                    if (!lamHH(s, H.st[k])) return false;
-                    pij = sub(p, H.pos[k]);
-                    x = sq(pij);
-                    return x != 0.0f && x <= P.Tlt_rh;
-                });
-                if (j < 0) break;
-                pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
-            }
-        }
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        {
-            Window w(L.off, P.dimL[0], csx, cex, csy, cey);
-            float2 pij = make_float2(0.f, 0.f);
-            float x = 0.0f;
-            for (;;) {
-                const int j = w.next([&](int k) {
-                    const unsigned sj = L.nst[k];
-                    if (!(lamHL(s, sj) && notDeleted(sj))) return false;
-                    pij = sub(p, L.pos[k]);
-                    x = sq(pij);
-                    return x != 0.0f && x <= P.Tlt_r;
-                });
-                if (j < 0) break;
-                pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
-            }
-        }
-        const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
-        acc.x *= -P.mH;
-        acc.y *= -P.mH;
-        accL.x *= -P.mL;
-        accL.y *= -P.mL;
-        acc.x -= P.sigma * accT.x;
-        acc.y -= P.sigma * accT.y;
-        acc.x += accL.x;
-        acc.y += accL.y;
-        acc.x += accB.x;
-        acc.y += accB.y;
-        acc.y -= P.g;
-        H.acc[i] = acc;
-        if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
-        v.x += P.dt * acc.x;
-        v.y += P.dt * acc.y;
-        p.x += P.dt * v.x;
-        p.y += P.dt * v.y;
-        // tether to the parent after the parent's advance (adjustPosition, 1007-1022)
-        const int id = H.id[i];
-        const int parent = id >> 2;
-        if (parent >= 0 && parent < P.slotsL) {
-            const int pi = L.map[parent];
-            if (pi >= 0 && L.st[pi] == 1) {
-                const float2 pl = L.npos[pi];
-                const float rho = L.dens[pi];
-                const float2 pji = sub(p, pl);
-                const float dist = vnorm(pji);
-                const float lim = static_cast<float>(
-                    fmin(static_cast<double>(dist),
-                         0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(rho) * kPi))));
-                p.x = pl.x + lim / dist * pji.x;
-                p.y = pl.y + lim / dist * pji.y;
-            }
-        }
-        H.npos[i] = p;
-        H.nvel[i] = v;
-        H.nst[i] = static_cast<uint8_t>(s);
-        H.nid[i] = id;
-        grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, cell_hash(p, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
-        if (H.ndens) {
-            H.ndens[i] = dens;
-            H.npres[i] = H.pres[i];
+        if constexpr (B) {
+            const Params P = V.table[V.scH[i]];
+            force_high_one(P, V, i);
+        } else {
+            force_high_one(P0, V, i);
         }
     }
 }
@@ -473,121 +542,148 @@ __global__ void __launch_bounds__(256, 6) k_force_high(Params P, StepView V) {
 // TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:2380-2446): density 1133-1217,
 // pressure + wall force 1499-1622 (= TwoScale2D/WCSPHSolver.cu:2035-2158), dt/10.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_relax_density(Params P, StepView V) {
-    const int nf = min(4 * V.cnt->n_fresh, P.capH);  // relaxation scratch holds capH entries
+__device__ __forceinline__ int fresh_child(const Params& P0, const StepView& V, int f) {
+    const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
+    return (slot >= 0 && slot < P0.slotsH) ? V.H.map[slot] : -1;
+}
+
+__device__ __forceinline__ void relax_density_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
+    const int* offH = H.off + P.cbH;
+    const int* offL = L.off + P.cbL;
+    const float2 p = H.pos[i];
+    float d = 0.0f, dl = 0.0f;
+    int csx, csy, cex, cey;
+    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    for (int cy = csy; cy <= cey; ++cy) {
+        const int row = cy * P.dimH[0];
+        const int b = offH[row + cex + 1];
+        for (int j = offH[row + csx]; j < b; ++j) {
+            float dist = vnorm(sub(p, H.pos[j]));
+            if (dist <= P.rh) d += kernW(dist, P.rh, P.CH);
+        }
+    }
+    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    for (int cy = csy; cy <= cey; ++cy) {
+        const int row = cy * P.dimL[0];
+        const int b = offL[row + cex + 1];
+        for (int j = offL[row + csx]; j < b; ++j) {
+            float dist = vnorm(sub(p, L.pos[j]));
+            if (dist <= P.rh) dl += kernW(dist, P.rh, P.CH);
+        }
+    }
+    d *= P.mH;
+    dl *= P.mL;
+    d += dl;
+    H.dens[i] = d;
+    H.pres[i] = tait(d, P);
+}
+
+template <bool B>
+__global__ void __launch_bounds__(256) k_relax_density(Params P0, StepView V) {
+    const int nf = min(4 * V.cnt->n_fresh, P0.capH);  // relaxation scratch holds capH entries
     for (int f = tid(); f < nf; f += nthreads()) {
-        const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
-        const int i = (slot >= 0 && slot < P.slotsH) ? H.map[slot] : -1;
+        const int i = fresh_child(P0, V, f);
         if (i < 0) continue;
-        const float2 p = H.pos[i];
-        float d = 0.0f, dl = 0.0f;
-        int csx, csy, cex, cey;
-        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimH[0];
-            const int b = H.off[row + cex + 1];
-            for (int j = H.off[row + csx]; j < b; ++j) {
-                float dist = vnorm(sub(p, H.pos[j]));
-                if (dist <= P.rh) d += kernW(dist, P.rh, P.CH);
-            }
+        if constexpr (B) {
+            const Params P = V.table[V.scH[i]];
+            relax_density_one(P, V, i);
+        } else {
+            relax_density_one(P0, V, i);
         }
-        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int b = L.off[row + cex + 1];
-            for (int j = L.off[row + csx]; j < b; ++j) {
-                float dist = vnorm(sub(p, L.pos[j]));
-                if (dist <= P.rh) dl += kernW(dist, P.rh, P.CH);
-            }
-        }
-        d *= P.mH;
-        dl *= P.mL;
-        d += dl;
-        H.dens[i] = d;
-        H.pres[i] = tait(d, P);
     }
 }
 
-__global__ void __launch_bounds__(256) k_relax_force(Params P, StepView V) {
-    const int nf = min(4 * V.cnt->n_fresh, P.capH);  // relaxation scratch holds capH entries
+__device__ __forceinline__ void relax_force_one(const Params& P, const StepView& V, int i, int f) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
+    const int* offH = H.off + P.cbH;
+    const int* offL = L.off + P.cbL;
+    const int* woff = V.woff + P.cbL;
+    float2 p = H.pos[i], v = H.vel[i];
+    const float dens = H.dens[i], pre = H.pres[i];
+    const float dens2 = dens * dens;
+    float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
+    int csx, csy, cex, cey;
+    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
+    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    for (int cy = csy; cy <= cey; ++cy) {
+        const int row = cy * P.dimH[0];
+        const int b = offH[row + cex + 1];
+        for (int j = offH[row + csx]; j < b; ++j) {
+            const float2 pij = sub(p, H.pos[j]);
+            const float dist = vnorm(pij);
+            if (dist != 0.0f && dist < P.rh) {
+                const float dj = H.dens[j];
+                const float coeff = pre / dens2 + H.pres[j] / (dj * dj);
+                const float2 g = kernDW(pij, dist, P.rh, P.GH);
+                acc.x += coeff * g.x;
+                acc.y += coeff * g.y;
+            }
+        }
+    }
+    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
+    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    for (int cy = csy; cy <= cey; ++cy) {
+        const int row = cy * P.dimL[0];
+        const int b = offL[row + cex + 1];
+        for (int j = offL[row + csx]; j < b; ++j) {
+            const float2 pij = sub(p, L.pos[j]);
+            const float dist = vnorm(pij);
+            if (dist != 0.0f && dist < P.rh) {
+                const float dj = L.dens[j];
+                const float coeff = pre / dens2 + L.pres[j] / (dj * dj);
+                const float2 g = kernDW(pij, dist, P.rh, P.GH);
+                accL.x += coeff * g.x;
+                accL.y += coeff * g.y;
+            }
+        }
+        const int wb = woff[row + cex + 1];
+        for (int k = woff[row + csx]; k < wb; ++k) {
+            const float2 pik = sub(p, V.wpos[k]);
+            const float gm = wall_weight(vnorm(pik), P.rh, P.cs);
+            accB.x += P.cBH * gm * pik.x;
+            accB.y += P.cBH * gm * pik.y;
+        }
+    }
+    acc.x *= -P.mH;
+    acc.y *= -P.mH;
+    accL.x *= -P.mL;
+    accL.y *= -P.mL;
+    acc.x += accL.x;
+    acc.y += accL.y;
+    acc.x += accB.x;
+    acc.y += accB.y;
+    v.x += P.relax_dt * acc.x;
+    v.y += P.relax_dt * acc.y;
+    p.x += P.relax_dt * v.x;
+    p.y += P.relax_dt * v.y;
+    V.relax_pos[f] = p;
+    V.relax_vel[f] = v;
+}
+
+template <bool B>
+__global__ void __launch_bounds__(256) k_relax_force(Params P0, StepView V) {
+    const int nf = min(4 * V.cnt->n_fresh, P0.capH);  // relaxation scratch holds capH entries
     for (int f = tid(); f < nf; f += nthreads()) {
-        const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
-        const int i = (slot >= 0 && slot < P.slotsH) ? H.map[slot] : -1;
+        const int i = fresh_child(P0, V, f);
         if (i < 0) continue;
-        float2 p = H.pos[i], v = H.vel[i];
-        const float dens = H.dens[i], pre = H.pres[i];
-        const float dens2 = dens * dens;
-        float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
-        int csx, csy, cex, cey;
-        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimH[0];
-            const int b = H.off[row + cex + 1];
-            for (int j = H.off[row + csx]; j < b; ++j) {
-                const float2 pij = sub(p, H.pos[j]);
-                const float dist = vnorm(pij);
-                if (dist != 0.0f && dist < P.rh) {
-                    const float dj = H.dens[j];
-                    const float coeff = pre / dens2 + H.pres[j] / (dj * dj);
-                    const float2 g = kernDW(pij, dist, P.rh, P.GH);
-                    acc.x += coeff * g.x;
-                    acc.y += coeff * g.y;
-                }
-            }
+        if constexpr (B) {
+            const Params P = V.table[V.scH[i]];
+            relax_force_one(P, V, i, f);
+        } else {
+            relax_force_one(P0, V, i, f);
         }
-        grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-        grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int b = L.off[row + cex + 1];
-            for (int j = L.off[row + csx]; j < b; ++j) {
-                const float2 pij = sub(p, L.pos[j]);
-                const float dist = vnorm(pij);
-                if (dist != 0.0f && dist < P.rh) {
-                    const float dj = L.dens[j];
-                    const float coeff = pre / dens2 + L.pres[j] / (dj * dj);
-                    const float2 g = kernDW(pij, dist, P.rh, P.GH);
-                    accL.x += coeff * g.x;
-                    accL.y += coeff * g.y;
-                }
-            }
-            const int wb = V.woff[row + cex + 1];
-            for (int k = V.woff[row + csx]; k < wb; ++k) {
-                const float2 pik = sub(p, V.wpos[k]);
-                const float gm = wall_weight(vnorm(pik), P.rh, P.cs);
-                accB.x += P.cBH * gm * pik.x;
-                accB.y += P.cBH * gm * pik.y;
-            }
-        }
-        acc.x *= -P.mH;
-        acc.y *= -P.mH;
-        accL.x *= -P.mL;
-        accL.y *= -P.mL;
-        acc.x += accL.x;
-        acc.y += accL.y;
-        acc.x += accB.x;
-        acc.y += accB.y;
-        v.x += P.relax_dt * acc.x;
-        v.y += P.relax_dt * acc.y;
-        p.x += P.relax_dt * v.x;
-        p.y += P.relax_dt * v.y;
-        V.relax_pos[f] = p;
-        V.relax_vel[f] = v;
     }
 }
 
-__global__ void k_relax_apply(Params P, StepView V) {
-    const int nf = min(4 * V.cnt->n_fresh, P.capH);  // relaxation scratch holds capH entries
+__global__ void k_relax_apply(Params P0, StepView V) {
+    const int nf = min(4 * V.cnt->n_fresh, P0.capH);  // relaxation scratch holds capH entries
     for (int f = tid(); f < nf; f += nthreads()) {
-        const int slot = 4 * V.split_ids[f >> 2] + (f & 3);
-        const int i = (slot >= 0 && slot < P.slotsH) ? V.H.map[slot] : -1;
+        const int i = fresh_child(P0, V, f);
         if (i < 0) continue;
         const_cast<float2*>(V.H.pos)[i] = V.relax_pos[f];
         const_cast<float2*>(V.H.vel)[i] = V.relax_vel[f];
@@ -605,5 +701,23 @@ __global__ void k_step_finish(Counters* c) {
         c->steps += 1;
     }
 }
+
+// Host-side launchers (the templates stay in this translation unit).
+#define TSS_LAUNCHER(NAME)                                                                        \
+    void launch_##NAME(bool batched, int blocks, int threads, cudaStream_t s, const Params& P,   \
+                       const StepView& V) {                                                       \
+        if (batched)                                                                              \
+            NAME<true><<<blocks, threads, 0, s>>>(P, V);                                          \
+        else                                                                                      \
+            NAME<false><<<blocks, threads, 0, s>>>(P, V);                                         \
+    }
+TSS_LAUNCHER(k_density_high)
+TSS_LAUNCHER(k_density_low)
+TSS_LAUNCHER(k_force_low)
+TSS_LAUNCHER(k_split)
+TSS_LAUNCHER(k_force_high)
+TSS_LAUNCHER(k_relax_density)
+TSS_LAUNCHER(k_relax_force)
+#undef TSS_LAUNCHER
 
 }  // namespace tss

@@ -43,20 +43,36 @@ struct StepView {
     float2* relax_pos;      // [capH] relaxation scratch
     float2* relax_vel;
     int nL;                 // low-res count (constant for a solver)
+    // batches only: per-scene parameters and each sorted particle's scene
+    const Params* table;
+    const uint16_t* scL;
+    const uint16_t* scH;
 };
 
 constexpr int kSplitThreads = 256;
 constexpr int kSplitItems = 16;
 constexpr int kSplitTile = kSplitThreads * kSplitItems;
 
-__global__ void k_density_high(Params P, StepView V);
-__global__ void k_density_low(Params P, StepView V);
-__global__ void k_force_low(Params P, StepView V);
-__global__ void k_split(Params P, StepView V);
-__global__ void k_force_high(Params P, StepView V);
-__global__ void k_relax_density(Params P, StepView V);
-__global__ void k_relax_force(Params P, StepView V);
-__global__ void k_relax_apply(Params P, StepView V);
+// B = false: one scene, parameters P0 (kernel constants).  B = true: a batch of
+// scenes; each particle's parameters are V.table[scene of the particle], and each
+// scene's grids sit at its cell bases in one global cell space.
+template <bool B> __global__ void k_density_high(Params P0, StepView V);
+template <bool B> __global__ void k_density_low(Params P0, StepView V);
+template <bool B> __global__ void k_force_low(Params P0, StepView V);
+template <bool B> __global__ void k_split(Params P0, StepView V);
+template <bool B> __global__ void k_force_high(Params P0, StepView V);
+template <bool B> __global__ void k_relax_density(Params P0, StepView V);
+template <bool B> __global__ void k_relax_force(Params P0, StepView V);
+__global__ void k_relax_apply(Params P0, StepView V);
 __global__ void k_step_finish(Counters* c);
+
+// host launchers of the templates above (batched selects B)
+void launch_k_density_high(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+void launch_k_density_low(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+void launch_k_force_low(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+void launch_k_split(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+void launch_k_force_high(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+void launch_k_relax_density(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+void launch_k_relax_force(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 
 }  // namespace tss

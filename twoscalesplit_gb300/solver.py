@@ -128,6 +128,48 @@ class Solver:
         return b
 
 
+class Batch(Solver):
+    """Many independent scenes advanced together (tss_batch_create): one grid build
+    and one launch of each kernel per step for all of them.  Each scene's results
+    equal those of the same scene run alone."""
+
+    def __init__(self, scenes, cap_high=None):
+        self.lib = load_library()
+        self.scenes = list(scenes)
+        self._keep = []
+        descs = (_abi.TssSceneDesc * len(self.scenes))()
+        for k, sc in enumerate(self.scenes):
+            lp = np.ascontiguousarray(sc.low_pos, np.float32).reshape(-1, 2)
+            lv = np.ascontiguousarray(sc.low_vel, np.float32).reshape(-1, 2)
+            wp = np.ascontiguousarray(sc.wall_pos, np.float32).reshape(-1, 2)
+            self._keep += [lp, lv, wp, sc.config]
+            descs[k] = _abi.TssSceneDesc(ctypes.pointer(sc.config), lp.shape[0], fptr(lp), fptr(lv), sc.mass_low,
+                                         sc.mass_high, wp.shape[0], fptr(wp), sc.mass_wall)
+        self.cap_high = int(cap_high if cap_high is not None else sum(sc.cap_high for sc in self.scenes))
+        self.n_low = sum(sc.n_low for sc in self.scenes)
+        h = ctypes.c_void_p()
+        check(self.lib.tss_batch_create(len(self.scenes), descs, self.cap_high, ctypes.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def scene_counts(self):
+        n = len(self.scenes)
+        lo = np.zeros(n, np.int32)
+        hi = np.zeros(n, np.int32)
+        self._check(self.lib.tss_solver_scene_counts(self.h, iptr(lo), iptr(hi)))
+        return lo, hi
+
+    def download_scene(self, scene, scale):
+        lo, hi = self.scene_counts()
+        n = int(lo[scene] if scale == TSS_SCALE_LOW else hi[scene])
+        out = {"id": np.zeros(n, np.int32), "pos": np.zeros((n, 2), np.float32), "vel": np.zeros((n, 2), np.float32),
+               "state": np.zeros(n, np.uint8), "dens": np.zeros(n, np.float32), "pres": np.zeros(n, np.float32)}
+        st = TssScaleState(n, iptr(out["id"]), fptr(out["pos"]), fptr(out["vel"]), u8ptr(out["state"]),
+                           fptr(out["dens"]), fptr(out["pres"]))
+        self._check(self.lib.tss_solver_download_scene(self.h, scene, scale, ctypes.byref(st)))
+        return out
+
+
 # ---------------------------------------------------------------------------
 # Reference-shaped interface
 # ---------------------------------------------------------------------------

@@ -66,6 +66,19 @@ def stage_bytes(stage, n_low, n_high, c_low, c_high, carry, n_fresh_children):
     return 0
 
 
+def measured_traffic(stage):
+    """DRAM bytes per launch of a stage's kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#") and parts[0] == stage:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
 def hbm_peak():
     try:
         with open(MEASURED_PEAKS) as f:
@@ -319,7 +332,8 @@ def run_ours(args):
                    "q1_compat": bool(cfg.flags & 1), "l2": "flushed between timed steps (512 MiB write)",
                    "parallelism": f"replicas{world}", "seed": 0},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
-                     "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": None,
+                     "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": measured_traffic(top),
+                     "traffic_source": "profiles/dram_traffic.txt (ncu, one launch)",
                      "algorithmic_bytes_per_launch": top_bytes, "launch_ms": st_avg[top],
                      "step": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (step_ms * 1e-3) / 1e9,
                               "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak}},
@@ -337,6 +351,73 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    """The mixed-size batch workload: `--scenes` independent scenes advanced in
+    lockstep by one batch (one grid build and one launch of each kernel per step),
+    against the same scenes advanced one at a time by the plain solver."""
+    import torch
+    from twoscalesplit_gb300 import build, scenes
+    from twoscalesplit_gb300.solver import Batch, Solver
+    build.build()
+    dev = torch.device("cuda", 0)
+    scs = scenes.mixed_batch(args.scenes, seed=0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    b = Batch(scs)
+    init = b.download(0)
+    empty = {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32), "vel": np.zeros((0, 2), np.float32),
+             "state": np.zeros(0, np.uint8)}
+    b.step(max(args.warmup, 1), stream=sh)
+    torch.cuda.synchronize(dev)
+    b.upload(0, init)
+    b.upload(1, empty)
+    b.set_fresh(np.zeros(0, np.int32))
+    K = args.steps
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = ClockSampler(None)
+    clocks.start()
+    for k in range(K):
+        flush.zero_()
+        evs[k][0].record(stream)
+        b.step(1, stream=sh)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    b.sync()
+    batch_ms = sum(x.elapsed_time(y) for x, y in evs)
+    c = b.counts()
+    parts_end = c["n_low"] + c["n_high"]
+    del b
+    # the plain solver, one scene at a time, same steps
+    plain_ms = 0.0
+    n_plain = min(len(scs), args.plain_sample)
+    for sc in scs[:n_plain]:
+        sol = Solver.from_scene(sc)
+        sol.step(max(args.warmup, 1), stream=sh)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sol.step(K, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        plain_ms += e0.elapsed_time(e1)
+        del sol
+    plain_ms *= len(scs) / n_plain
+    n_low = sum(sc.n_low for sc in scs)
+    line = {"metric": "scene-steps/s", "value": len(scs) * K / (batch_ms / 1e3), "unit": "scene-steps/s",
+            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": batch_ms / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"mixed_batch_{len(scs)}", "scenes": len(scs), "n_low_total": n_low,
+                       "n_high_end": c["n_high"], "l2": "flushed between timed steps (512 MiB write)"},
+            "particle_steps_per_s": n_low * K / (batch_ms / 1e3),
+            "plain_one_at_a_time": {"scene_steps_per_s": len(scs) * K / (plain_ms / 1e3),
+                                    "sampled_scenes": n_plain, "ms_per_lockstep": plain_ms / K},
+            "speedup_vs_plain": plain_ms / batch_ms, "clocks": clk, "n_particles_end": parts_end}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -346,8 +427,13 @@ def main():
     ap.add_argument("--scene", default="dam_break_1m")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch"])
+    ap.add_argument("--scenes", type=int, default=512)
+    ap.add_argument("--plain-sample", type=int, default=64)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "batch":
+        run_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -159,6 +159,66 @@ def dam_break_small(nx, ny, dx=None, seed=0, roi=None, relax_iters=4, cap_high=N
                       cap_high if cap_high is not None else 4 * nx * ny, relax_iters, seed, **kw)
 
 
+def _box_scene(name, fluid, dx, roi, steps, cap_factor, seed_rng, relax_iters=0, calibrate_mass=True):
+    """A scene in the unit box from fluid lattice points (before jitter)."""
+    dx = float(np.float32(dx))
+    low = fluid + seed_rng.uniform(-1e-4 * dx, 1e-4 * dx, size=fluid.shape)
+    low = low.astype(np.float32)
+    wdx = 0.5 * dx
+    nw = int(math.ceil(1.0 / wdx)) + 1
+    walls = particle_box_canvas(0.0, 0.0, wdx, nw, nw, 3, 3)
+    pad = 4 * wdx
+    r = 2.0 * dx
+    cfg = config_init(-pad, -pad, (nw - 1) * wdx + pad, (nw - 1) * wdx + pad, r, 0.5 * r,
+                      REST_DENSITY, TAIT_B, SPEED_SOUND, ALPHA, SIGMA, 1e-4 * dx / 0.008)
+    cfg.roi[:] = roi
+    cfg.relax_iters = relax_iters
+    m = REST_DENSITY * dx * dx
+    if calibrate_mass:
+        m = REST_DENSITY / lattice_pair_kernel_sum(dx, float(cfg.r_low), float(cfg.r_high))
+    n = low.shape[0]
+    return Scene(name=name, config=cfg, low_pos=low, low_vel=np.zeros_like(low), mass_low=m, mass_high=m / 4.0,
+                 cap_high=int(cap_factor * n), wall_pos=walls, mass_wall=REST_DENSITY * wdx * wdx, steps=steps,
+                 dx=dx)
+
+
+def mixed_scene(rng, n_min=2000, n_max=200000, steps=1000, cap_factor=4.0):
+    """One scene of the mixed-size batch workload: a dam break (block width
+    U[0.2,0.5], height U[0.4,0.9]) or a droplet (radius U[0.1,0.3], centre height
+    U[0.5,0.8]) above a pool of depth U[0.1,0.4]; low-res count log-uniform in
+    [n_min, n_max]; spacing from the count and the fluid area; the region of
+    interest a rectangle covering U[10%,40%] of the box at a uniform position; dt
+    at the Courant number of dam_break_5k; mass calibrated to rest density."""
+    n_target = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
+    if rng.uniform() < 0.5:
+        w, h = rng.uniform(0.2, 0.5), rng.uniform(0.4, 0.9)
+        dx = math.sqrt(w * h / n_target)
+        nx, ny = max(1, int(round(w / dx))), max(1, int(round(h / dx)))
+        fluid = particle_box(0.5 * dx, 0.5 * dx, dx, nx, ny).astype(np.float64)
+        kind = "dam"
+    else:
+        rad, cy, depth = rng.uniform(0.1, 0.3), rng.uniform(0.5, 0.8), rng.uniform(0.1, 0.4)
+        dx = math.sqrt((math.pi * rad * rad + depth) / n_target)
+        n1 = int(math.ceil(1.0 / dx))
+        g = particle_box(0.5 * dx, 0.5 * dx, dx, n1, n1).astype(np.float64)
+        g = g[(g[:, 0] < 1.0) & (g[:, 1] < 1.0)]
+        pool = g[:, 1] < depth
+        drop = ((g[:, 0] - 0.5) ** 2 + (g[:, 1] - cy) ** 2 < rad * rad) & (g[:, 1] > depth + dx)
+        fluid = g[pool | drop]
+        kind = "droplet"
+    frac = rng.uniform(0.1, 0.4)
+    aw = min(1.0, math.sqrt(frac) * rng.uniform(0.7, 1.4))
+    ah = min(1.0, frac / aw)
+    x0, y0 = rng.uniform(0.0, 1.0 - aw), rng.uniform(0.0, 1.0 - ah)
+    return _box_scene(f"{kind}_{fluid.shape[0]}", fluid, dx, [x0, y0, x0 + aw, y0 + ah], steps, cap_factor, rng)
+
+
+def mixed_batch(n_scenes=512, seed=0, **kw):
+    """The batch workload: n_scenes independent mixed scenes (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [mixed_scene(rng, **kw) for _ in range(n_scenes)]
+
+
 SCENES = {"dam_break_5k": dam_break_5k, "dam_break_1m": dam_break_1m}
 
 

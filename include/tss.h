@@ -117,9 +117,10 @@ typedef struct tss_scene_desc {
  * so one grid build and one launch of each kernel advance all of them; a scene's
  * results are the same as when it runs alone (the reference's solver held one
  * scene per process, WCSPHSolver.cu:2728).  The returned handle works with every
- * tss_solver_* call; slot ids are global (scene k's low-res particle i is
- * sum_{j<k} n_low_j + i); tss_solver_download_scene returns one scene with its
- * own ids. */
+ * tss_solver_* call; slot ids are global (scene k's low-res particle i has slot
+ * base_k + i, base_k a multiple of TSS_POOL_SLOT_PAGE); tss_solver_download_scene
+ * returns one scene with its own ids.  A batch is a pool (below) sized for exactly
+ * these scenes, with scene k admitted as scene k. */
 tss_status tss_batch_create(int n_scenes, const tss_scene_desc* scenes, int cap_high, tss_solver** out);
 tss_status tss_solver_num_scenes(tss_solver* s, int* n_scenes);
 /* Per-scene particle counts (arrays of n_scenes ints, either may be NULL). */
@@ -127,6 +128,136 @@ tss_status tss_solver_scene_counts(tss_solver* s, int* n_low, int* n_high);
 /* One scene's state, scene-local ids (low: 0..n_low-1, high: 4*low id + child). */
 struct tss_scale_state;
 tss_status tss_solver_download_scene(tss_solver* s, int scene, int scale, struct tss_scale_state* out);
+
+/* ------------------------------------------------------------------------- */
+/* Pools: scenes admitted and retired between steps (continuous batching)       */
+/* ------------------------------------------------------------------------- */
+/* No counterpart in the reference (one scene per process).  A pool is a batch
+ * whose device arrays are sized once, for capacities, and whose scenes come and
+ * go between steps: tss_pool_admit places a scene in free pages of each resource,
+ * tss_pool_retire frees them, and tss_solver_step advances every admitted scene
+ * together (the step is one CUDA graph for the pool's capacities; the work of each
+ * kernel follows the particles and cells in use).  A scene's results do not
+ * depend on what else is in the pool or where it was placed.  All calls that take
+ * a stream are ordered on it; use the same stream for tss_solver_step. */
+#define TSS_POOL_SLOT_PAGE 256   /* low-res slots per page (high-res slots: 4x) */
+#define TSS_POOL_CELL_PAGE 64    /* grid cells per page, both scales */
+#define TSS_POOL_WALL_PAGE 64    /* wall particles per page */
+#define TSS_POOL_MAX_SCENES 65535
+
+typedef struct tss_pool_config {
+    int64_t low_slots;       /* low-res particles over all admitted scenes */
+    int64_t high_particles;  /* high-res list capacity; each admission reserves 4 per low-res particle */
+    int64_t low_cells;       /* low-res grid cells (a scene takes its grid's cells + 1) */
+    int64_t high_cells;      /* high-res grid cells */
+    int64_t wall_particles;
+    int32_t max_scenes;      /* <= TSS_POOL_MAX_SCENES */
+    int32_t relax_iters;     /* every admitted scene's config must have this relax_iters */
+} tss_pool_config;
+
+/* What a scene takes from a pool (host only; rounded to pages). */
+typedef struct tss_footprint {
+    int64_t low_slots, high_particles, low_cells, high_cells, wall_particles;
+} tss_footprint;
+
+/* Device bytes of a pool (host only, no device needed). */
+tss_status tss_pool_bytes(const tss_pool_config* cfg, size_t* bytes);
+/* The largest pool of `bytes` device bytes whose resources are in the given
+ * proportions per low-res slot (high-res list 4 per slot; low_cells_per_slot
+ * low-res cells, 4x that high-res; walls_per_slot walls).  Host only. */
+tss_status tss_pool_config_for_budget(size_t bytes, double low_cells_per_slot, double walls_per_slot,
+                                      int max_scenes, int relax_iters, tss_pool_config* out);
+tss_status tss_scene_footprint(const tss_scene_desc* scene, tss_footprint* out);
+
+tss_status tss_pool_create(const tss_pool_config* cfg, tss_solver** out);
+/* Place a scene and enqueue its upload, grid keys and wall grid on `stream`.
+ * TSS_CAPACITY: some resource has no free run large enough now (retry after a
+ * retirement); TSS_INVALID_ARG: the scene can never fit this pool, or its
+ * relax_iters differs.  Pageable host arrays are copied before the call returns;
+ * page-locked ones are read by the stream and must stay unchanged until it has
+ * passed the admission. */
+tss_status tss_pool_admit(tss_solver* s, const tss_scene_desc* scene, void* stream, int* scene_id);
+/* Would tss_pool_admit succeed now?  TSS_OK, TSS_CAPACITY or TSS_INVALID_ARG as
+ * it would return, without admitting anything. */
+tss_status tss_pool_can_admit(tss_solver* s, const tss_scene_desc* scene);
+/* Drop a scene's particles from the next grid build and free its pages at once
+ * (the pages may be admitted to again before the next step). */
+tss_status tss_pool_retire(tss_solver* s, int scene_id, void* stream);
+/* Resources free now (host-side accounting). */
+tss_status tss_pool_free(tss_solver* s, tss_footprint* free_now);
+
+/* A scene's state in caller memory: arrays of each scale (0 low, 1 high) with
+ * capacities cap[k]; NULL arrays are skipped; ids are scene-local.  n[] is what a
+ * host-side call wrote. */
+typedef struct tss_scene_result {
+    int32_t cap[2];
+    int32_t n[2];
+    int32_t* id[2];
+    float* pos[2];     /* 2 floats per particle */
+    float* vel[2];
+    uint8_t* state[2];
+    float* dens[2];    /* density of the last step (0 for children created in it) */
+    float* pres[2];
+} tss_scene_result;
+
+/* Enqueue a copy of an admitted scene's state after its last step into `dst`,
+ * whose arrays must be device-accessible (device memory or mapped page-locked
+ * host memory) and 8-byte aligned; d_counts (2 device-accessible ints) receives
+ * the particles of each scale.  Valid between a step and the next one, before
+ * the scene's retirement; cap[0] >= n_low and cap[1] >= 4 n_low always suffice.
+ * Order within each scale: the list order (the last step's (cell, id) order,
+ * then that step's new children). */
+tss_status tss_pool_extract(tss_solver* s, int scene_id, const tss_scene_result* dst, int32_t* d_counts,
+                            void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Serving: a request loop over a pool                                           */
+/* ------------------------------------------------------------------------- */
+/* Replays a trace of scene requests in real time: a request is visible from its
+ * arrival time on, is admitted (first come, first served) as soon as the pool
+ * has room for it, advances with every other admitted scene, and after `horizon`
+ * steps its final state is extracted, copied to `result` and its pages freed.
+ * Steps are issued in chunks that end when some scene reaches its horizon (at
+ * most max_steps_per_launch), so admission and retirement happen between steps
+ * while the GPU works on the chunks queued before. */
+typedef struct tss_server tss_server;
+typedef struct tss_server_config {
+    tss_pool_config pool;
+    int32_t max_steps_per_launch;   /* e.g. 8 */
+    int32_t max_in_flight;          /* chunks queued ahead of the GPU, e.g. 2 */
+    int64_t staging_bytes;          /* page-locked staging for uploads and results */
+} tss_server_config;
+
+typedef struct tss_request {
+    tss_scene_desc scene;
+    int32_t horizon;            /* steps, >= 1 */
+    double arrival_s;           /* seconds after the start of tss_server_run */
+    tss_scene_result* result;   /* host arrays for the final state, or NULL */
+} tss_request;
+
+typedef struct tss_request_stats {
+    double arrival_s;
+    double admit_s;             /* host time of the admission call */
+    double done_s;              /* the final state is in host memory (GPU event time) */
+    int64_t first_step;         /* pool step index of the scene's first step */
+    int32_t status;             /* TSS_OK, or TSS_INVALID_ARG if it can never fit */
+    int32_t n_low, n_high;      /* final counts */
+} tss_request_stats;
+
+typedef struct tss_serve_summary {
+    double makespan_s;          /* trace start to the last result */
+    int64_t steps;              /* pool steps launched */
+    int64_t scene_steps;        /* sum of the served requests' horizons */
+    double low_particle_steps;  /* sum of n_low * horizon */
+    double mean_active;         /* scenes per step, averaged over steps */
+    int32_t max_active;
+    int32_t served;
+} tss_serve_summary;
+
+tss_status tss_server_create(const tss_server_config* cfg, tss_server** out);
+tss_status tss_server_run(tss_server* sv, int n, const tss_request* reqs, tss_request_stats* stats,
+                          tss_serve_summary* summary);
+void tss_server_destroy(tss_server* sv);
 
 /* Advance n_steps steps (WCSPHSolver::AdvanceTS, WCSPHSolver.cu:2726-2810), enqueued
  * on `stream` (a cudaStream_t; NULL = the default stream, as the reference used).

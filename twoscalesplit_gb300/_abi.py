@@ -101,6 +101,59 @@ class TssSceneDesc(ctypes.Structure):
                 ("wall_pos", ctypes.POINTER(ctypes.c_float)), ("mass_wall", ctypes.c_float)]
 
 
+TSS_POOL_SLOT_PAGE = 256
+TSS_POOL_CELL_PAGE = 64
+TSS_POOL_WALL_PAGE = 64
+TSS_POOL_MAX_SCENES = 65535
+
+
+class TssPoolConfig(ctypes.Structure):
+    """struct tss_pool_config (include/tss.h)."""
+    _fields_ = [("low_slots", ctypes.c_int64), ("high_particles", ctypes.c_int64), ("low_cells", ctypes.c_int64),
+                ("high_cells", ctypes.c_int64), ("wall_particles", ctypes.c_int64), ("max_scenes", ctypes.c_int32),
+                ("relax_iters", ctypes.c_int32)]
+
+
+class TssFootprint(ctypes.Structure):
+    _fields_ = [("low_slots", ctypes.c_int64), ("high_particles", ctypes.c_int64), ("low_cells", ctypes.c_int64),
+                ("high_cells", ctypes.c_int64), ("wall_particles", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class TssSceneResult(ctypes.Structure):
+    """struct tss_scene_result: arrays of each scale (0 low, 1 high)."""
+    _fields_ = [("cap", ctypes.c_int32 * 2), ("n", ctypes.c_int32 * 2), ("id", ctypes.c_void_p * 2),
+                ("pos", ctypes.c_void_p * 2), ("vel", ctypes.c_void_p * 2), ("state", ctypes.c_void_p * 2),
+                ("dens", ctypes.c_void_p * 2), ("pres", ctypes.c_void_p * 2)]
+
+
+class TssServerConfig(ctypes.Structure):
+    _fields_ = [("pool", TssPoolConfig), ("max_steps_per_launch", ctypes.c_int32), ("max_in_flight", ctypes.c_int32),
+                ("staging_bytes", ctypes.c_int64)]
+
+
+class TssRequest(ctypes.Structure):
+    _fields_ = [("scene", TssSceneDesc), ("horizon", ctypes.c_int32), ("arrival_s", ctypes.c_double),
+                ("result", ctypes.POINTER(TssSceneResult))]
+
+
+class TssRequestStats(ctypes.Structure):
+    _fields_ = [("arrival_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("first_step", ctypes.c_int64), ("status", ctypes.c_int32), ("n_low", ctypes.c_int32),
+                ("n_high", ctypes.c_int32)]
+
+
+class TssServeSummary(ctypes.Structure):
+    _fields_ = [("makespan_s", ctypes.c_double), ("steps", ctypes.c_int64), ("scene_steps", ctypes.c_int64),
+                ("low_particle_steps", ctypes.c_double), ("mean_active", ctypes.c_double),
+                ("max_active", ctypes.c_int32), ("served", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class TssBuffers(ctypes.Structure):
     _fields_ = [("pos", ctypes.c_void_p * 2), ("vel", ctypes.c_void_p * 2), ("dens", ctypes.c_void_p * 2),
                 ("id", ctypes.c_void_p * 2), ("state", ctypes.c_void_p * 2), ("counts", ctypes.c_void_p)]
@@ -179,6 +232,20 @@ def load_library(path=None):
         "tss_solver_download_scene": (i, [vp, i, i, ctypes.POINTER(TssScaleState)]),
         "tss_grid_build": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp, ctypes.c_size_t, vp]),
         "tss_grid_build_noalloc": (i, [vp, vp, i, f, f, f, i, i, vp, vp, vp]),
+        "tss_pool_bytes": (i, [ctypes.POINTER(TssPoolConfig), ctypes.POINTER(ctypes.c_size_t)]),
+        "tss_pool_config_for_budget": (i, [ctypes.c_size_t, ctypes.c_double, ctypes.c_double, i, i,
+                                           ctypes.POINTER(TssPoolConfig)]),
+        "tss_scene_footprint": (i, [ctypes.POINTER(TssSceneDesc), ctypes.POINTER(TssFootprint)]),
+        "tss_pool_create": (i, [ctypes.POINTER(TssPoolConfig), ctypes.POINTER(vp)]),
+        "tss_pool_admit": (i, [vp, ctypes.POINTER(TssSceneDesc), vp, ctypes.POINTER(i)]),
+        "tss_pool_can_admit": (i, [vp, ctypes.POINTER(TssSceneDesc)]),
+        "tss_pool_retire": (i, [vp, i, vp]),
+        "tss_pool_free": (i, [vp, ctypes.POINTER(TssFootprint)]),
+        "tss_pool_extract": (i, [vp, i, ctypes.POINTER(TssSceneResult), vp, vp]),
+        "tss_server_create": (i, [ctypes.POINTER(TssServerConfig), ctypes.POINTER(vp)]),
+        "tss_server_run": (i, [vp, i, ctypes.POINTER(TssRequest), ctypes.POINTER(TssRequestStats),
+                               ctypes.POINTER(TssServeSummary)]),
+        "tss_server_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -13,8 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtss.so")
-SOURCES = ["grid.cu", "grid_noalloc.cu", "sph.cu", "solver.cu"]
-HEADERS = ["tss_device.cuh", "grid.cuh", "sph.cuh"]
+SOURCES = ["grid.cu", "grid_noalloc.cu", "sph.cu", "solver.cu", "pool.cu", "serve.cpp"]
+HEADERS = ["tss_device.cuh", "grid.cuh", "sph.cuh", "solver_impl.cuh", "extent.hpp"]
 ARCH = os.environ.get("TSS_CUDA_ARCH", "103a")
 
 
@@ -48,7 +48,7 @@ def build(force=False, verbose=False, ptxas_info=False):
     procs = []
     objs = []
     for src in SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [cc, *flags(), "-c", os.path.join(CSRC, src), "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")

@@ -7,7 +7,7 @@
 
 namespace tss {
 
-int particle_blocks(int cap, int threads) {
+int sm_count() {
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -15,8 +15,12 @@ int particle_blocks(int cap, int threads) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 152;
     }
+    return sms;
+}
+
+int particle_blocks(int cap, int threads) {
     long long need = (static_cast<long long>(cap) + threads - 1) / threads;
-    long long lim = static_cast<long long>(sms) * 16;
+    long long lim = static_cast<long long>(sm_count()) * 16;
     long long b = need < lim ? need : lim;
     return b < 1 ? 1 : static_cast<int>(b);
 }
@@ -29,93 +33,110 @@ __global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restric
         grid_key(count, key, rank, tile_sum, i, cell_hash(pos[i], ox, oy, cell, dimx, dimy));
 }
 
-// One tile of kScanTile counts per block.  The tile's offset is the sum of the
-// tile sums before it (a few hundred, read from L2), so tiles are independent and
-// nothing waits on another block.  Counts are zeroed for the next key pass (only
-// the 16-byte groups that hold a non-zero count are written back).
+// Tiles of kScanTile counts, strided over the blocks.  A tile's offset is the sum
+// of the tile sums before it (read from L2), so tiles are independent and nothing
+// waits on another block.  Only the cells in use are scanned (a pool's grids are
+// sized for its capacity); counts are zeroed for the next key pass (only the
+// 16-byte groups that hold a non-zero count are written back).
 __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
     __shared__ unsigned s_warp[kScanThreads / 32];
     __shared__ unsigned s_red[kScanThreads / 32];
-    const int tile = blockIdx.x;
-    const int C = g.ncells;
+    const int C = g.used ? min(*g.used, g.ncells) : g.ncells;
+    const int ntiles = (C + kScanTile - 1) / kScanTile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned before = 0;
-    for (int t = threadIdx.x; t < tile; t += blockDim.x) before += g.tile_sum[t];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
-    if (lane == 0) s_red[warp] = before;
-    const int base = tile * kScanTile + threadIdx.x * kScanItems;
-    unsigned v[kScanItems];
-    const bool full = base + kScanItems <= C;
-    if (full) {
-        uint4* p = reinterpret_cast<uint4*>(g.count + base);
-#pragma unroll
-        for (int q = 0; q < kScanItems / 4; ++q) {
-            const uint4 a = p[q];
-            v[4 * q] = a.x;
-            v[4 * q + 1] = a.y;
-            v[4 * q + 2] = a.z;
-            v[4 * q + 3] = a.w;
-            if (a.x | a.y | a.z | a.w) p[q] = make_uint4(0, 0, 0, 0);
+    if (C <= 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            g.off[0] = 0;
+            *g.total = 0;
         }
-    } else {
+        return;
+    }
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        unsigned before = 0;
+        for (int t = threadIdx.x; t < tile; t += blockDim.x) before += g.tile_sum[t];
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            int idx = base + k;
-            v[k] = idx < C ? g.count[idx] : 0u;
-            if (idx < C && v[k]) g.count[idx] = 0u;
+        for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+        if (lane == 0) s_red[warp] = before;
+        const int base = tile * kScanTile + threadIdx.x * kScanItems;
+        unsigned v[kScanItems];
+        const bool full = base + kScanItems <= C;
+        if (full) {
+            uint4* p = reinterpret_cast<uint4*>(g.count + base);
+#pragma unroll
+            for (int q = 0; q < kScanItems / 4; ++q) {
+                const uint4 a = p[q];
+                v[4 * q] = a.x;
+                v[4 * q + 1] = a.y;
+                v[4 * q + 2] = a.z;
+                v[4 * q + 3] = a.w;
+                if (a.x | a.y | a.z | a.w) p[q] = make_uint4(0, 0, 0, 0);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k) {
+                int idx = base + k;
+                v[k] = idx < C ? g.count[idx] : 0u;
+                if (idx < C && v[k]) g.count[idx] = 0u;
+            }
         }
-    }
-    unsigned sum = 0;
+        unsigned sum = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) sum += v[k];
-    unsigned inc = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) s_warp[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
-        unsigned r = lane < kScanThreads / 32 ? s_red[lane] : 0u;
-        unsigned wi = w;
+        for (int k = 0; k < kScanItems; ++k) sum += v[k];
+        unsigned inc = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += t;
+            unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
         }
+        if (lane == 31) s_warp[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+            unsigned r = lane < kScanThreads / 32 ? s_red[lane] : 0u;
+            unsigned wi = w;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-        if (lane < kScanThreads / 32) s_warp[lane] = wi - w + r;  // exclusive warp offsets + tile prefix
-    }
-    __syncthreads();
-    unsigned run = s_warp[warp] + (inc - sum);
-    if (full) {
-        int4* q = reinterpret_cast<int4*>(g.off + base);
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
 #pragma unroll
-        for (int k = 0; k < kScanItems / 4; ++k) {
-            int4 o4;
-            o4.x = static_cast<int>(run);
-            run += v[4 * k];
-            o4.y = static_cast<int>(run);
-            run += v[4 * k + 1];
-            o4.z = static_cast<int>(run);
-            run += v[4 * k + 2];
-            o4.w = static_cast<int>(run);
-            run += v[4 * k + 3];
-            q[k] = o4;
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+            if (lane < kScanThreads / 32) s_warp[lane] = wi - w + r;  // exclusive warp offsets + tile prefix
         }
-        if (base + kScanItems == C) g.off[C] = static_cast<int>(run);
-    } else {
+        __syncthreads();
+        unsigned run = s_warp[warp] + (inc - sum);
+        if (full) {
+            int4* q = reinterpret_cast<int4*>(g.off + base);
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            int idx = base + k;
-            if (idx < C) g.off[idx] = static_cast<int>(run);
-            run += v[k];
-            if (idx == C - 1) g.off[C] = static_cast<int>(run);
+            for (int k = 0; k < kScanItems / 4; ++k) {
+                int4 o4;
+                o4.x = static_cast<int>(run);
+                run += v[4 * k];
+                o4.y = static_cast<int>(run);
+                run += v[4 * k + 1];
+                o4.z = static_cast<int>(run);
+                run += v[4 * k + 2];
+                o4.w = static_cast<int>(run);
+                run += v[4 * k + 3];
+                q[k] = o4;
+            }
+            if (base + kScanItems == C) {
+                g.off[C] = static_cast<int>(run);
+                *g.total = static_cast<int>(run);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k) {
+                int idx = base + k;
+                if (idx < C) g.off[idx] = static_cast<int>(run);
+                run += v[k];
+                if (idx == C - 1) {
+                    g.off[C] = static_cast<int>(run);
+                    *g.total = static_cast<int>(run);
+                }
+            }
         }
+        __syncthreads();  // s_warp / s_red are reused by the next tile
     }
 }
 
@@ -125,9 +146,16 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
 __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
                                unsigned* err) {
     const int n = *n_ptr;
+    const int total = *g.total;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int dst = g.off[g.key[i]] + g.rank[i];
-        if (dst < 0 || dst >= n) {
+        const int c = g.key[i];
+        if (c < 0) continue;  // dropped from the list
+        if (c >= g.ncells) {
+            atomicOr(err, kErrTimeout);
+            continue;
+        }
+        const int dst = g.off[c] + g.rank[i];
+        if (dst < 0 || dst >= total) {
             atomicOr(err, kErrTimeout);
             continue;
         }
@@ -135,16 +163,23 @@ __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __r
     }
 }
 
-__global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err) {
-    const int n = *n_ptr;
+// The sorted entries are [0, total); the list count *n_ptr becomes total (only
+// block 0 writes it, and nothing in this kernel reads it).
+__global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, unsigned* err) {
+    const int n = *g.total;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_ptr = n;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         int2 pe = g.perm[k];
         const int src = pe.x, id = pe.y;
-        if (src < 0 || src >= n) {
+        if (src < 0 || src >= cap) {
             atomicOr(err, kErrTimeout);
             continue;
         }
         const int c = g.key[src];
+        if (c < 0 || c >= g.ncells) {
+            atomicOr(err, kErrTimeout);
+            continue;
+        }
         const int s = g.off[c], e = g.off[c + 1];
         if (s < 0 || e > n || s > k || k >= e) {
             atomicOr(err, kErrTimeout);
@@ -166,7 +201,7 @@ __global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, Reorde
             a.dst_pres[dst] = a.src_pres[src];
         }
         if (a.dst_order) a.dst_order[dst] = src;
-        if (a.dst_sc) a.dst_sc[dst] = static_cast<uint16_t>(scene_of_slot(a.slot_base, a.nscenes, id >> a.id_shift));
+        if (a.dst_sc) a.dst_sc[dst] = a.page_scene[(id >> a.id_shift) >> a.page_shift];
         if (a.slot_map) {
             if (id >= 0 && id < a.slots) a.slot_map[id] = dst;
             else atomicOr(err, kErrTimeout);
@@ -179,7 +214,8 @@ size_t grid_bufs_bytes(int cap, int ncells) {
     int ntiles = (ncells + kScanTile - 1) / kScanTile;
     if (ntiles < 1) ntiles = 1;
     return al(sizeof(unsigned) * (size_t)ncells) + al(sizeof(int) * ((size_t)ncells + 1)) +
-           al(sizeof(int) * (size_t)cap) * 2 + al(sizeof(int2) * (size_t)cap) + al(sizeof(unsigned) * (size_t)ntiles);
+           al(sizeof(int) * (size_t)cap) * 2 + al(sizeof(int2) * (size_t)cap) + al(sizeof(unsigned) * (size_t)ntiles) +
+           256;
 }
 
 GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
@@ -200,6 +236,9 @@ GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
     g.perm = reinterpret_cast<int2*>(p);
     p += al(sizeof(int2) * (size_t)cap);
     g.tile_sum = reinterpret_cast<unsigned*>(p);
+    p += al(sizeof(unsigned) * (size_t)g.ntiles);
+    g.used = nullptr;
+    g.total = reinterpret_cast<int*>(p);
     return g;
 }
 
@@ -211,19 +250,20 @@ cudaError_t grid_keys_enqueue(const float2* pos, const int* n_ptr, int cap, floa
     return cudaGetLastError();
 }
 
-cudaError_t grid_sort_enqueue(const int32_t* id, const int* n_ptr, int cap, GridBufs g, ReorderArgs a,
+cudaError_t grid_sort_enqueue(const int32_t* id, int* n_ptr, int cap, GridBufs g, ReorderArgs a,
                               unsigned* err, cudaStream_t stream) {
     const int T = 256;
     const int pb = particle_blocks(cap, T);
+    const int sb = g.ntiles < 8 * sm_count() ? g.ntiles : 8 * sm_count();
     cudaError_t e;
-    k_grid_scan<<<g.ntiles, kScanThreads, 0, stream>>>(g);
+    k_grid_scan<<<sb, kScanThreads, 0, stream>>>(g);
     if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
     k_grid_scatter<<<pb, T, 0, stream>>>(n_ptr, id, g, err);
-    k_grid_reorder<<<pb, T, 0, stream>>>(n_ptr, g, a, err);
+    k_grid_reorder<<<pb, T, 0, stream>>>(n_ptr, cap, g, a, err);
     return cudaGetLastError();
 }
 
-cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
+cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, int* n_ptr, int cap, float ox, float oy,
                                float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
                                cudaStream_t stream) {
     cudaError_t e;

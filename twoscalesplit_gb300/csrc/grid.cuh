@@ -12,11 +12,14 @@
 //   k_grid_keys     key[i] = cell(pos[i]); rank[i] = atomicAdd(&count[cell], 1);
 //                   per tile of kScanTile cells, the number of particles
 //                   (warp-aggregated atomics), so the scan needs no look-back
-//   k_grid_scan     off = exclusive_scan(count): each tile adds the sums of the
-//                   tiles before it; count is zeroed for the next build; off[C] = n
-//   k_grid_scatter  perm[off[key[i]] + rank[i]] = (i, id[i])
+//   k_grid_scan     off = exclusive_scan(count) over the cells in use: each tile
+//                   adds the sums of the tiles before it; count is zeroed for the
+//                   next build; off[used] = total = the number of keyed entries
+//   k_grid_scatter  perm[off[key[i]] + rank[i]] = (i, id[i]); entries whose key is
+//                   negative (removed since their key pass) are dropped
 //   k_grid_reorder  each sorted slot counts the smaller ids of its cell to find its
-//                   final place and gathers the particle's state there (SoA reorder)
+//                   final place and gathers the particle's state there (SoA reorder);
+//                   the list count becomes the sorted count
 #pragma once
 #include "tss_device.cuh"
 
@@ -30,11 +33,14 @@ struct GridBufs {
     int ncells;             // C
     unsigned* count;        // [C], zero between builds
     int* off;               // [C+1]
-    int* key;               // [cap] cell of list entry i
+    int* key;               // [cap] cell of list entry i (negative: entry dropped at the next build)
     int* rank;              // [cap]
     int2* perm;             // [cap] (list index, id) in cell order (atomic order inside a cell)
     unsigned* tile_sum;     // [ntiles] particles per tile of kScanTile cells (zero between builds)
     int ntiles;
+    const int* used;        // device int: cells [0, used) can hold entries (null: all C); the
+                            // scan covers only those, so its cost follows the cells in use
+    int* total;             // device int: entries sorted by the last build
 };
 
 // What the reorder moves: list-order arrays (src) into sorted-order arrays (dst).
@@ -53,11 +59,11 @@ struct ReorderArgs {
     int32_t* dst_order;        // may be null: source list index of each sorted position
     int32_t* slot_map;         // may be null: slot id -> sorted index
     int slots;                 // size of slot_map
-    // batches: the scene of each sorted entry, found from its slot id
-    // (slot_base[s] <= id >> id_shift < slot_base[s + 1])
+    // batches: the scene of each sorted entry, page_scene[(id >> id_shift) >> page_shift]
+    // (scenes own whole pages of low-res slots)
     uint16_t* dst_sc;          // may be null
-    const int* slot_base;      // [nscenes + 1], ascending
-    int nscenes;
+    const uint16_t* page_scene;
+    int page_shift;
     int id_shift;              // 0 for low-res ids, 2 for high-res (4 children per parent)
     int* h_state0;             // may be null: set to 1 if some entry has (state & 1) == 0
 };
@@ -66,25 +72,14 @@ __global__ void k_grid_keys(const float2* __restrict__ pos, const int* __restric
                             float cell, int dimx, int dimy, unsigned* __restrict__ count, int* __restrict__ key,
                             int* __restrict__ rank, unsigned* __restrict__ tile_sum);
 __global__ void k_grid_scan(GridBufs g);
-// Scene of a slot id: the s with slot_base[s] <= low_slot < slot_base[s + 1].
-__device__ __forceinline__ int scene_of_slot(const int* __restrict__ slot_base, int nscenes, int low_slot) {
-    int lo = 0, hi = nscenes - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (slot_base[mid] <= low_slot) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
                                unsigned* err);
-__global__ void k_grid_reorder(const int* __restrict__ n_ptr, GridBufs g, ReorderArgs a, unsigned* err);
+__global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, unsigned* err);
 
 // Enqueue a whole build: clears the counts and tile sums, then keys, scan,
 // scatter, reorder.  `n_ptr` is a device int <= cap; inconsistent offsets set
 // kErrTimeout in *err.
-cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* n_ptr, int cap, float ox, float oy,
+cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, int* n_ptr, int cap, float ox, float oy,
                                float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
                                cudaStream_t stream);
 // The key pass alone (counts and tile sums must be zero), and the rest of a build
@@ -93,7 +88,7 @@ cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, const int* 
 // only the rest here.
 cudaError_t grid_keys_enqueue(const float2* pos, const int* n_ptr, int cap, float ox, float oy, float cell, int dimx,
                               int dimy, GridBufs g, cudaStream_t stream);
-cudaError_t grid_sort_enqueue(const int32_t* id, const int* n_ptr, int cap, GridBufs g, ReorderArgs a,
+cudaError_t grid_sort_enqueue(const int32_t* id, int* n_ptr, int cap, GridBufs g, ReorderArgs a,
                               unsigned* err, cudaStream_t stream);
 
 // The key of list entry i for the next build: its cell, its rank among the cell's
@@ -112,6 +107,7 @@ size_t grid_bufs_bytes(int cap, int ncells);
 GridBufs grid_bufs_carve(void* base, int cap, int ncells);
 
 int particle_blocks(int cap, int threads);
+int sm_count();
 __global__ void k_set_int(int* p, int v);
 
 }  // namespace tss

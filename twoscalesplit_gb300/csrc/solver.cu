@@ -1,13 +1,6 @@
-// solver.cu -- host side of the solver behind the C ABI (include/tss.h).
-//
-// Replaces WCSPHSolver + ParticleSystem's device storage (TwoScale2D/WCSPHSolver.cu:
-// 2287-3238, TwoScale2D/ParticleSystem.cpp:13-119).  Differences by design:
-//  * one device arena per solver, all state resident; no GL interop
-//  * the particle counts stay on the device (no per-step readback, 2760-2781);
-//    every kernel reads its count from device memory
-//  * a whole step is captured once into a CUDA graph and replayed
-//  * all handle state is per handle (the reference kept activeID in a function
-//    static, 2728)
+// solver.cu -- host side of the solver behind the C ABI (include/tss.h): the step
+// sequence, single-scene creation and the calls common to every handle.  Pools and
+// batches of scenes are in pool.cu; the handle itself is in solver_impl.cuh.
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
@@ -17,246 +10,153 @@
 #include <string>
 #include <vector>
 
-#include <cuda_runtime.h>
-
-#include "../../include/tss.h"
-#include "grid.cuh"
-#include "sph.cuh"
+#include "solver_impl.cuh"
 
 using namespace tss;
 
-namespace {
-
-struct ScaleBufs {
-    float2 *pos, *vel, *acc, *npos, *nvel;
-    uint8_t *st, *nst;
-    int32_t *id, *nid, *map;
-    float *dens, *pres, *q, *ndens, *npres;
-    GridBufs g;
-};
-
-size_t al(size_t x) { return (x + 255) & ~size_t(255); }
-
-struct Arena {
-    std::vector<std::pair<void**, size_t>> items;
-    template <class T>
-    void add(T** p, size_t count) { items.push_back({reinterpret_cast<void**>(p), al(sizeof(T) * (count ? count : 1))}); }
-    size_t total() const {
-        size_t t = 0;
-        for (auto& it : items) t += it.second;
-        return t;
+StepView tss_solver::view() const {
+    StepView v{};
+    auto sv = [](const ScaleBufs& b) {
+        ScaleView s{};
+        s.pos = b.pos;
+        s.vel = b.vel;
+        s.st = b.st;
+        s.id = b.id;
+        s.dens = b.dens;
+        s.pres = b.pres;
+        s.q = b.q;
+        s.acc = b.acc;
+        s.off = b.g.off;
+        s.map = b.map;
+        s.npos = b.npos;
+        s.nvel = b.nvel;
+        s.nst = b.nst;
+        s.nid = b.nid;
+        s.ndens = b.ndens;
+        s.npres = b.npres;
+        s.gcount = b.g.count;
+        s.gkey = b.g.key;
+        s.grank = b.g.rank;
+        s.gtile = b.g.tile_sum;
+        return s;
+    };
+    v.L = sv(L);
+    v.H = sv(H);
+    if (!carry) {
+        v.L.ndens = v.L.npres = nullptr;
+        v.H.ndens = v.H.npres = nullptr;
     }
-    void carve(char* base) {
-        for (auto& it : items) {
-            *it.first = base;
-            base += it.second;
-        }
+    v.wpos = wpos;
+    v.woff = woff;
+    v.cnt = cnt;
+    v.split_flag = split_flag;
+    v.split_ids = split_ids;
+    v.split_tile = split_tile;
+    v.relax_pos = relax_pos;
+    v.relax_vel = relax_vel;
+    v.nL = nL;
+    v.table = d_table;
+    v.scL = scL;
+    v.scH = scH;
+    return v;
+}
+
+ReorderArgs tss_solver::reorder_args(ScaleBufs& b, bool high) {
+    ReorderArgs a{};
+    a.src_pos = b.npos;
+    a.src_vel = b.nvel;
+    a.src_st = b.nst;
+    a.dst_pos = b.pos;
+    a.dst_vel = b.vel;
+    a.dst_st = b.st;
+    a.dst_id = b.id;
+    a.slot_map = b.map;
+    a.slots = high ? slotsH : slotsL;
+    if (carry) {
+        a.src_dens = b.ndens;
+        a.src_pres = b.npres;
+        a.dst_dens = b.dens;
+        a.dst_pres = b.pres;
     }
-};
-
-}  // namespace
-
-struct tss_solver {
-    tss_config cfg;
-    Params P;
-    int nL = 0, capH = 0, slotsL = 0, slotsH = 0, nW = 0;
-    int CL = 0, CH = 0;
-    bool carry = false;
-    bool batched = false;  // a batch of scenes (tss_batch_create)
-    char* arena = nullptr;
-    ScaleBufs L{}, H{};
-    float2* wpos = nullptr;
-    int* woff = nullptr;
-    Counters* cnt = nullptr;
-    uint8_t* split_flag = nullptr;
-    int32_t* split_ids = nullptr;
-    unsigned* split_tile = nullptr;
-    int split_ntiles = 1;
-    float2* relax_pos = nullptr;
-    float2* relax_vel = nullptr;
-    cudaStream_t stream = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    int blocksL = 1, blocksH = 1;
-    bool uploaded[2] = {false, false};  // state replaced since the last step
-    int S = 1;                          // scenes
-    std::vector<Params> h_table;        // per-scene parameters (host copy)
-    std::vector<int> h_slot_base;       // [S + 1] first low-res slot of each scene
-    Params* d_table = nullptr;
-    int* d_slot_base = nullptr;
-    uint16_t* scL = nullptr;            // batches: scene of each sorted particle
-    uint16_t* scH = nullptr;
-    bool profile = false;
-    cudaEvent_t ev[TSS_NUM_STAGES + 1] = {};
-    std::string err;
-
-    tss_status fail(tss_status st, const std::string& msg) {
-        err = msg;
-        return st;
+    if (high) a.h_state0 = &cnt->h_state0;
+    if (batched) {
+        a.dst_sc = high ? scH : scL;
+        a.page_scene = page_scene;
+        a.page_shift = 8;  // log2(TSS_POOL_SLOT_PAGE)
+        a.id_shift = high ? 2 : 0;
     }
-    tss_status cuda_fail(cudaError_t e, const char* where) {
-        err = std::string(where) + ": " + cudaGetErrorString(e);
-        return e == cudaErrorMemoryAllocation ? TSS_OOM : TSS_CUDA_ERROR;
-    }
+    return a;
+}
 
-    StepView view() const {
-        StepView v{};
-        auto sv = [](const ScaleBufs& b) {
-            ScaleView s{};
-            s.pos = b.pos;
-            s.vel = b.vel;
-            s.st = b.st;
-            s.id = b.id;
-            s.dens = b.dens;
-            s.pres = b.pres;
-            s.q = b.q;
-            s.acc = b.acc;
-            s.off = b.g.off;
-            s.map = b.map;
-            s.npos = b.npos;
-            s.nvel = b.nvel;
-            s.nst = b.nst;
-            s.nid = b.nid;
-            s.ndens = b.ndens;
-            s.npres = b.npres;
-            s.gcount = b.g.count;
-            s.gkey = b.g.key;
-            s.grank = b.g.rank;
-            s.gtile = b.g.tile_sum;
-            return s;
-        };
-        v.L = sv(L);
-        v.H = sv(H);
-        if (!carry) {
-            v.L.ndens = v.L.npres = nullptr;
-            v.H.ndens = v.H.npres = nullptr;
-        }
-        v.wpos = wpos;
-        v.woff = woff;
-        v.cnt = cnt;
-        v.split_flag = split_flag;
-        v.split_ids = split_ids;
-        v.split_tile = split_tile;
-        v.relax_pos = relax_pos;
-        v.relax_vel = relax_vel;
-        v.nL = nL;
-        v.table = d_table;
-        v.scL = scL;
-        v.scH = scH;
-        return v;
-    }
+// cudaEventRecordExternal makes the record a node of the captured graph (a plain
+// record inside capture only orders streams)
+cudaError_t tss_solver::mark(int k, cudaStream_t s) {
+    return profile ? cudaEventRecordWithFlags(ev[k], s, cudaEventRecordExternal) : cudaSuccess;
+}
 
-    ReorderArgs reorder_args(ScaleBufs& b, bool high) {
-        ReorderArgs a{};
-        a.src_pos = b.npos;
-        a.src_vel = b.nvel;
-        a.src_st = b.nst;
-        a.dst_pos = b.pos;
-        a.dst_vel = b.vel;
-        a.dst_st = b.st;
-        a.dst_id = b.id;
-        a.slot_map = b.map;
-        a.slots = high ? slotsH : slotsL;
-        if (carry) {
-            a.src_dens = b.ndens;
-            a.src_pres = b.npres;
-            a.dst_dens = b.dens;
-            a.dst_pres = b.pres;
-        }
-        if (high) a.h_state0 = &cnt->h_state0;
-        if (batched) {
-            a.dst_sc = high ? scH : scL;
-            a.slot_base = d_slot_base;
-            a.nscenes = S;
-            a.id_shift = high ? 2 : 0;
-        }
-        return a;
+// Enqueue one step (the body of AdvanceTS, WCSPHSolver.cu:2726-2810).
+cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
+    cudaError_t e;
+    const StepView V = view();
+    if ((e = mark(0, s)) != cudaSuccess) return e;
+    // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid);
+    //    their key pass ran at the end of the previous step (force kernels, split),
+    //    in prime_keys() after the state was set, or in a pool admission
+    e = grid_sort_enqueue(H.nid, &cnt->cur[1], capH, H.g, reorder_args(H, true), &cnt->err, s);
+    if (e != cudaSuccess || (e = mark(1, s)) != cudaSuccess) return e;
+    e = grid_sort_enqueue(L.nid, &cnt->cur[0], nL, L.g, reorder_args(L, false), &cnt->err, s);
+    if (e != cudaSuccess || (e = mark(2, s)) != cudaSuccess) return e;
+    // 2. relaxation of last step's children (older snapshot's relaxTransient)
+    for (int it = 0; it < P.relax_iters; ++it) {
+        launch_k_relax_density(batched, blocksH, 256, s, P, V);
+        launch_k_relax_force(batched, blocksH, 256, s, P, V);
+        k_relax_apply<<<blocksH, 256, 0, s>>>(P, V);
     }
+    if ((e = mark(3, s)) != cudaSuccess) return e;
+    // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
+    launch_k_density_high(batched, blocksH, 256, s, P, V);
+    if ((e = mark(4, s)) != cudaSuccess) return e;
+    launch_k_density_low(batched, blocksL, 256, s, P, V);
+    if ((e = mark(5, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
+    launch_k_force_low(batched, blocksL, 256, s, P, V);
+    if ((e = mark(6, s)) != cudaSuccess) return e;
+    launch_k_split(batched, std::min(split_ntiles, 8 * sm_count()), kSplitThreads, s, P, V);
+    if ((e = mark(7, s)) != cudaSuccess) return e;
+    launch_k_force_high(batched, blocksH, 256, s, P, V);
+    k_step_finish<<<1, 32, 0, s>>>(cnt);
+    if ((e = mark(8, s)) != cudaSuccess) return e;
+    return cudaGetLastError();
+}
 
-    // Enqueue one step (the body of AdvanceTS, WCSPHSolver.cu:2726-2810).
-    // cudaEventRecordExternal makes the record a node of the captured graph (a plain
-    // record inside capture only orders streams)
-    cudaError_t mark(int k, cudaStream_t s) {
-        return profile ? cudaEventRecordWithFlags(ev[k], s, cudaEventRecordExternal) : cudaSuccess;
+// Key pass of both grids for the current list arrays (after create or upload).
+cudaError_t tss_solver::prime_keys(cudaStream_t s) {
+    cudaError_t e;
+    for (ScaleBufs* b : {&L, &H}) {
+        if ((e = cudaMemsetAsync(b->g.count, 0, sizeof(unsigned) * static_cast<size_t>(b->g.ncells), s)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaMemsetAsync(b->g.tile_sum, 0, sizeof(unsigned) * b->g.ntiles, s)) != cudaSuccess) return e;
     }
-
-    cudaError_t enqueue_step(cudaStream_t s) {
-        cudaError_t e;
-        const StepView V = view();
-        if ((e = mark(0, s)) != cudaSuccess) return e;
-        // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid);
-        //    their key pass ran at the end of the previous step (force kernels, split)
-        //    or in prime_keys() after the state was set
-        e = grid_sort_enqueue(H.nid, &cnt->cur[1], capH, H.g, reorder_args(H, true), &cnt->err, s);
-        if (e != cudaSuccess || (e = mark(1, s)) != cudaSuccess) return e;
-        e = grid_sort_enqueue(L.nid, &cnt->cur[0], nL, L.g, reorder_args(L, false), &cnt->err, s);
-        if (e != cudaSuccess || (e = mark(2, s)) != cudaSuccess) return e;
-        // 2. relaxation of last step's children (older snapshot's relaxTransient)
-        for (int it = 0; it < P.relax_iters; ++it) {
-            launch_k_relax_density(batched, blocksH, 256, s, P, V);
-            launch_k_relax_force(batched, blocksH, 256, s, P, V);
-            k_relax_apply<<<blocksH, 256, 0, s>>>(P, V);
-        }
-        if ((e = mark(3, s)) != cudaSuccess) return e;
-        // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
-        launch_k_density_high(batched, blocksH, 256, s, P, V);
-        if ((e = mark(4, s)) != cudaSuccess) return e;
-        launch_k_density_low(batched, blocksL, 256, s, P, V);
-        if ((e = mark(5, s)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
-        launch_k_force_low(batched, blocksL, 256, s, P, V);
-        if ((e = mark(6, s)) != cudaSuccess) return e;
-        launch_k_split(batched, split_ntiles, kSplitThreads, s, P, V);
-        if ((e = mark(7, s)) != cudaSuccess) return e;
-        launch_k_force_high(batched, blocksH, 256, s, P, V);
-        k_step_finish<<<1, 32, 0, s>>>(cnt);
-        if ((e = mark(8, s)) != cudaSuccess) return e;
+    if (batched) {
+        launch_keys_batched(H.npos, H.nid, &cnt->cur[1], capH, d_table, page_scene, 8, 2, 1, H.g, s);
+        launch_keys_batched(L.npos, L.nid, &cnt->cur[0], nL, d_table, page_scene, 8, 0, 0, L.g, s);
         return cudaGetLastError();
     }
-
-    // Key pass of both grids for the current list arrays (after create or upload).
-    cudaError_t prime_keys(cudaStream_t s) {
-        cudaError_t e;
-        for (ScaleBufs* b : {&L, &H}) {
-            if ((e = cudaMemsetAsync(b->g.count, 0, sizeof(unsigned) * static_cast<size_t>(b->g.ncells), s)) !=
-                cudaSuccess)
-                return e;
-            if ((e = cudaMemsetAsync(b->g.tile_sum, 0, sizeof(unsigned) * b->g.ntiles, s)) != cudaSuccess) return e;
-        }
-        if (batched) {
-            k_keys_batched_launch(s);
-            return cudaGetLastError();
-        }
-        e = grid_keys_enqueue(H.npos, &cnt->cur[1], capH, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], H.g, s);
-        if (e != cudaSuccess) return e;
-        return grid_keys_enqueue(L.npos, &cnt->cur[0], nL, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], L.g, s);
-    }
-
-    void k_keys_batched_launch(cudaStream_t s);
-
-    void drop_graph() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        exec = nullptr;
-        graph = nullptr;
-    }
-
-    ~tss_solver() {
-        drop_graph();
-        for (auto& x : ev)
-            if (x) cudaEventDestroy(x);
-        if (stream) cudaStreamDestroy(stream);
-        if (arena) cudaFree(arena);
-    }
-};
+    e = grid_keys_enqueue(H.npos, &cnt->cur[1], capH, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], H.g, s);
+    if (e != cudaSuccess) return e;
+    return grid_keys_enqueue(L.npos, &cnt->cur[0], nL, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], L.g, s);
+}
 
 namespace {
 
 __global__ void k_iota(int32_t* p, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
 }
-__global__ void k_fill_i32(int32_t* p, int n, int v) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+__global__ void k_fill_i32(int32_t* p, int64_t n, int v) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        p[i] = v;
 }
 __global__ void k_set_counts(Counters* c, int nL, int nH) {
     c->cur[0] = c->next[0] = nL;
@@ -264,6 +164,21 @@ __global__ void k_set_counts(Counters* c, int nL, int nH) {
     c->h_state0 = 0;
 }
 __global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
+
+// Key pass of a pool's list: each entry's parameters come from the scene owning
+// its slot's page.
+__global__ void k_keys_batched(const float2* __restrict__ pos, const int32_t* __restrict__ id,
+                               const int* __restrict__ n_ptr, const Params* __restrict__ table,
+                               const uint16_t* __restrict__ page_scene, int page_shift, int shift, int high,
+                               GridBufs g) {
+    const int n = *n_ptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Params& P = table[page_scene[(id[i] >> shift) >> page_shift]];
+        const int c = high ? P.cbH + cell_hash(pos[i], P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1])
+                           : P.cbL + cell_hash(pos[i], P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]);
+        grid_key(g.count, g.key, g.rank, g.tile_sum, i, c);
+    }
+}
 
 // Largest x with sqrtf(x) <= r (le) or sqrtf(x) < r (lt).  IEEE square root is
 // correctly rounded and monotone on the host and (with -prec-sqrt=true) on the
@@ -286,6 +201,85 @@ bool finite_cfg(const tss_config* c) {
 }
 
 }  // namespace
+
+namespace tss {
+
+void launch_fill_i32(int32_t* p, int64_t n, int v, cudaStream_t s) {
+    if (n <= 0) return;
+    const int b = particle_blocks(n < (1LL << 30) ? static_cast<int>(n) : (1 << 30), 256);
+    k_fill_i32<<<b, 256, 0, s>>>(p, n, v);
+}
+void launch_iota(int32_t* p, int n, cudaStream_t s) {
+    if (n > 0) k_iota<<<particle_blocks(n, 256), 256, 0, s>>>(p, n);
+}
+void launch_set_counts(Counters* c, int nL, int nH, cudaStream_t s) { k_set_counts<<<1, 1, 0, s>>>(c, nL, nH); }
+void launch_keys_batched(const float2* pos, const int32_t* id, const int* n_ptr, int cap, const Params* table,
+                         const uint16_t* page_scene, int page_shift, int shift, int high, GridBufs g, cudaStream_t s) {
+    k_keys_batched<<<particle_blocks(cap > 0 ? cap : 1, 256), 256, 0, s>>>(pos, id, n_ptr, table, page_scene,
+                                                                           page_shift, shift, high, g);
+}
+
+bool valid_cfg(const tss_config* cfg) {
+    if (!cfg || !finite_cfg(cfg) || cfg->dims_low[0] <= 0 || cfg->dims_low[1] <= 0 || cfg->dims_high[0] <= 0 ||
+        cfg->dims_high[1] <= 0 || !(cfg->r_low > 0) || !(cfg->r_high > 0) || cfg->relax_iters < 0 ||
+        cfg->relax_iters > 64 || !(cfg->relax_dt_div > 0))
+        return false;
+    return static_cast<long long>(cfg->dims_low[0]) * cfg->dims_low[1] < (1LL << 31) - 2 &&
+           static_cast<long long>(cfg->dims_high[0]) * cfg->dims_high[1] < (1LL << 31) - 2;
+}
+
+// Per-scene constants, as Bind() derives them (WCSPHSolver.cu:2537-2611).
+Params make_params(const SceneIn& sc) {
+    const tss_config* cfg = sc.cfg;
+    Params P{};
+    P.ox = cfg->domain_origin[0];
+    P.oy = cfg->domain_origin[1];
+    P.dimL[0] = cfg->dims_low[0];
+    P.dimL[1] = cfg->dims_low[1];
+    P.dimH[0] = cfg->dims_high[0];
+    P.dimH[1] = cfg->dims_high[1];
+    P.r = cfg->r_low;
+    P.rh = cfg->r_high;
+    P.rho0 = cfg->rest_density;
+    P.B = cfg->tait_b;
+    P.cs = cfg->speed_sound;
+    P.alpha = cfg->alpha;
+    P.sigma = cfg->tension;
+    P.dt = cfg->dt;
+    P.g = cfg->gravity;
+    const double r = cfg->r_low, rh = cfg->r_high;  // Bind(), 2559-2590
+    P.CL = static_cast<float>(20.0 / (14.0 * kPi * r * r));
+    P.GL = static_cast<float>(-120.0 / (14.0 * kPi * r * r * r));
+    P.CH = static_cast<float>(20.0 / (14.0 * kPi * rh * rh));
+    P.GH = static_cast<float>(-120.0 / (14.0 * kPi * rh * rh * rh));
+    P.mL = sc.mass_low;
+    P.mH = sc.mass_high;
+    P.mB = sc.mass_wall;
+    P.cBL = sc.mass_wall / (sc.mass_low + sc.mass_wall);
+    P.cBH = sc.mass_wall / (sc.mass_high + sc.mass_wall);
+    P.hx = (cfg->r_low + cfg->r_high) / 2.0f;
+    P.relax_dt = cfg->dt / cfg->relax_dt_div;
+    for (int k = 0; k < 4; ++k) P.roi[k] = cfg->roi[k];
+    P.relax_iters = cfg->relax_iters;
+    P.q1 = (cfg->flags & TSS_FLAG_Q1_COMPAT) ? 1 : 0;
+    P.Tle_r = sq_cutoff(P.r, true);
+    P.Tlt_r = sq_cutoff(P.r, false);
+    P.Tle_rh = sq_cutoff(P.rh, true);
+    P.Tlt_rh = sq_cutoff(P.rh, false);
+    P.nLs = sc.n_low;
+    P.CHs = cfg->dims_high[0] * cfg->dims_high[1];
+    return P;
+}
+
+void scene_runs(const SceneIn& sc, tss_footprint* f) {
+    f->low_slots = sc.n_low;
+    f->high_particles = 4LL * sc.n_low;
+    f->low_cells = static_cast<int64_t>(sc.cfg->dims_low[0]) * sc.cfg->dims_low[1] + 1;
+    f->high_cells = static_cast<int64_t>(sc.cfg->dims_high[0]) * sc.cfg->dims_high[1];
+    f->wall_particles = sc.n_wall;
+}
+
+}  // namespace tss
 
 extern "C" {
 
@@ -341,155 +335,32 @@ tss_status tss_config_init(tss_config* cfg, float xs, float ys, float xe, float 
 
 namespace {
 
-struct SceneIn {
-    const tss_config* cfg;
-    int n_low;
-    const float* low_pos;
-    const float* low_vel;
-    float mass_low, mass_high;
-    int n_wall;
-    const float* wall_pos;
-    float mass_wall;
-};
-
-bool valid_cfg(const tss_config* cfg) {
-    if (!cfg || !finite_cfg(cfg) || cfg->dims_low[0] <= 0 || cfg->dims_low[1] <= 0 || cfg->dims_high[0] <= 0 ||
-        cfg->dims_high[1] <= 0 || !(cfg->r_low > 0) || !(cfg->r_high > 0) || cfg->relax_iters < 0 ||
-        cfg->relax_iters > 64 || !(cfg->relax_dt_div > 0))
-        return false;
-    return static_cast<long long>(cfg->dims_low[0]) * cfg->dims_low[1] < (1LL << 31) - 1 &&
-           static_cast<long long>(cfg->dims_high[0]) * cfg->dims_high[1] < (1LL << 31) - 1;
-}
-
-// Per-scene constants, as Bind() derives them (WCSPHSolver.cu:2537-2611).
-Params make_params(const SceneIn& sc) {
-    const tss_config* cfg = sc.cfg;
-    Params P{};
-    P.ox = cfg->domain_origin[0];
-    P.oy = cfg->domain_origin[1];
-    P.dimL[0] = cfg->dims_low[0];
-    P.dimL[1] = cfg->dims_low[1];
-    P.dimH[0] = cfg->dims_high[0];
-    P.dimH[1] = cfg->dims_high[1];
-    P.r = cfg->r_low;
-    P.rh = cfg->r_high;
-    P.rho0 = cfg->rest_density;
-    P.B = cfg->tait_b;
-    P.cs = cfg->speed_sound;
-    P.alpha = cfg->alpha;
-    P.sigma = cfg->tension;
-    P.dt = cfg->dt;
-    P.g = cfg->gravity;
-    const double r = cfg->r_low, rh = cfg->r_high;  // Bind(), 2559-2590
-    P.CL = static_cast<float>(20.0 / (14.0 * kPi * r * r));
-    P.GL = static_cast<float>(-120.0 / (14.0 * kPi * r * r * r));
-    P.CH = static_cast<float>(20.0 / (14.0 * kPi * rh * rh));
-    P.GH = static_cast<float>(-120.0 / (14.0 * kPi * rh * rh * rh));
-    P.mL = sc.mass_low;
-    P.mH = sc.mass_high;
-    P.mB = sc.mass_wall;
-    P.cBL = sc.mass_wall / (sc.mass_low + sc.mass_wall);
-    P.cBH = sc.mass_wall / (sc.mass_high + sc.mass_wall);
-    P.hx = (cfg->r_low + cfg->r_high) / 2.0f;
-    P.relax_dt = cfg->dt / cfg->relax_dt_div;
-    for (int k = 0; k < 4; ++k) P.roi[k] = cfg->roi[k];
-    P.relax_iters = cfg->relax_iters;
-    P.q1 = (cfg->flags & TSS_FLAG_Q1_COMPAT) ? 1 : 0;
-    P.Tle_r = sq_cutoff(P.r, true);
-    P.Tlt_r = sq_cutoff(P.r, false);
-    P.Tle_rh = sq_cutoff(P.rh, true);
-    P.Tlt_rh = sq_cutoff(P.rh, false);
-    P.nLs = sc.n_low;
-    P.CHs = cfg->dims_high[0] * cfg->dims_high[1];
-    return P;
-}
-
-__global__ void k_keys_batched(const float2* __restrict__ pos, const int32_t* __restrict__ id,
-                               const int* __restrict__ n_ptr, const Params* __restrict__ table,
-                               const int* __restrict__ slot_base, int nscenes, int shift, int high, GridBufs g) {
-    const int n = *n_ptr;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const Params& P = table[scene_of_slot(slot_base, nscenes, id[i] >> shift)];
-        const int c = high ? P.cbH + cell_hash(pos[i], P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1])
-                           : P.cbL + cell_hash(pos[i], P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]);
-        grid_key(g.count, g.key, g.rank, g.tile_sum, i, c);
-    }
-}
-
-__global__ void k_wall_keys(const float2* __restrict__ pos, const uint16_t* __restrict__ wsc, int n,
-                            const Params* __restrict__ table, GridBufs g) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const Params& P = table[wsc[i]];
-        grid_key(g.count, g.key, g.rank, g.tile_sum, i, P.cbL + cell_hash(pos[i], P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
-    }
-}
-
-}  // namespace
-
-void tss_solver::k_keys_batched_launch(cudaStream_t st) {
-    k_keys_batched<<<particle_blocks(capH > 0 ? capH : 1, 256), 256, 0, st>>>(H.npos, H.nid, &cnt->cur[1], d_table,
-                                                                               d_slot_base, S, 2, 1, H.g);
-    k_keys_batched<<<particle_blocks(nL > 0 ? nL : 1, 256), 256, 0, st>>>(L.npos, L.nid, &cnt->cur[0], d_table,
-                                                                           d_slot_base, S, 0, 0, L.g);
-}
-
-namespace {
-
-tss_status create_solver(const std::vector<SceneIn>& scenes, int cap_high, bool batched, tss_solver** out) {
+// A single scene (tss_solver_create); pools and batches are created in pool.cu.
+tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
     if (!out) return TSS_INVALID_ARG;
     *out = nullptr;
-    const int S = static_cast<int>(scenes.size());
-    if (S < 1 || S > 65535 || cap_high < 0) return TSS_INVALID_ARG;
-    long long nL_ll = 0, nW_ll = 0, CL_ll = 0, CH_ll = 0;
-    for (const SceneIn& sc : scenes) {
-        if (!valid_cfg(sc.cfg) || sc.n_low < 0 || sc.n_wall < 0) return TSS_INVALID_ARG;
-        if ((sc.n_low > 0 && !sc.low_pos) || (sc.n_wall > 0 && !sc.wall_pos)) return TSS_INVALID_ARG;
-        if (sc.cfg->relax_iters != scenes[0].cfg->relax_iters) return TSS_INVALID_ARG;  // one graph for all
-        nL_ll += sc.n_low;
-        nW_ll += sc.n_wall;
-        CL_ll += static_cast<long long>(sc.cfg->dims_low[0]) * sc.cfg->dims_low[1];
-        CH_ll += static_cast<long long>(sc.cfg->dims_high[0]) * sc.cfg->dims_high[1];
-    }
-    if (4 * nL_ll >= (1LL << 31) - 1 || nW_ll >= (1LL << 31) - 1 || CL_ll >= (1LL << 31) - 2 ||
-        CH_ll >= (1LL << 31) - 2)
-        return TSS_INVALID_ARG;
+    if (!valid_cfg(sc.cfg) || sc.n_low < 0 || sc.n_wall < 0 || cap_high < 0) return TSS_INVALID_ARG;
+    if ((sc.n_low > 0 && !sc.low_pos) || (sc.n_wall > 0 && !sc.wall_pos)) return TSS_INVALID_ARG;
+    if (4LL * sc.n_low >= (1LL << 31) - 1) return TSS_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return TSS_NO_DEVICE;
 
     tss_solver* s = new (std::nothrow) tss_solver();
     if (!s) return TSS_OOM;
-    const int n_low = static_cast<int>(nL_ll), n_wall = static_cast<int>(nW_ll);
-    s->cfg = *scenes[0].cfg;
-    s->batched = batched;
+    const int n_low = sc.n_low, n_wall = sc.n_wall;
+    s->cfg = *sc.cfg;
     s->nL = n_low;
     s->capH = cap_high;
     s->slotsL = n_low;
     s->slotsH = 4 * n_low;
     s->nW = n_wall;
-    s->CL = static_cast<int>(CL_ll);
-    s->CH = static_cast<int>(CH_ll);
-    s->carry = scenes[0].cfg->relax_iters > 0;
-    s->S = S;
-    // per-scene parameters, cell bases and slot bases
-    int cbL = 0, cbH = 0, sbL = 0;
-    s->h_table.resize(S);
-    s->h_slot_base.resize(S + 1);
-    for (int k = 0; k < S; ++k) {
-        Params P = make_params(scenes[k]);
-        P.cbL = batched ? cbL : 0;
-        P.cbH = batched ? cbH : 0;
-        P.sbL = batched ? sbL : 0;
-        P.slotsL = s->slotsL;
-        P.slotsH = s->slotsH;
-        P.capH = cap_high;
-        s->h_table[k] = P;
-        s->h_slot_base[k] = sbL;
-        cbL += scenes[k].cfg->dims_low[0] * scenes[k].cfg->dims_low[1];
-        cbH += P.CHs;
-        sbL += scenes[k].n_low;
-    }
-    s->h_slot_base[S] = sbL;
-    s->P = s->h_table[0];
+    s->CL = sc.cfg->dims_low[0] * sc.cfg->dims_low[1];
+    s->CH = sc.cfg->dims_high[0] * sc.cfg->dims_high[1];
+    s->carry = sc.cfg->relax_iters > 0;
+    s->P = make_params(sc);
+    s->P.slotsL = s->slotsL;
+    s->P.slotsH = s->slotsH;
+    s->P.capH = cap_high;
 
     // ---- one arena for everything ----
     Arena A;
@@ -520,11 +391,9 @@ tss_status create_solver(const std::vector<SceneIn>& scenes, int cap_high, bool 
     A.add(&gW, grid_bufs_bytes(n_wall > 0 ? n_wall : 1, s->CL));
     float2* wraw = nullptr;
     int32_t* wid = nullptr;
-    uint16_t* wsc = nullptr;
     A.add(&s->wpos, n_wall);
     A.add(&wraw, n_wall);
     A.add(&wid, n_wall);
-    A.add(&wsc, batched ? n_wall : 1);
     A.add(&s->cnt, 1);
     int* nW_dev = nullptr;
     A.add(&nW_dev, 4);
@@ -534,16 +403,13 @@ tss_status create_solver(const std::vector<SceneIn>& scenes, int cap_high, bool 
     A.add(&s->split_tile, s->split_ntiles);
     A.add(&s->relax_pos, s->carry ? cap_high : 1);
     A.add(&s->relax_vel, s->carry ? cap_high : 1);
-    A.add(&s->d_table, S);
-    A.add(&s->d_slot_base, S + 1);
-    A.add(&s->scL, batched ? n_low : 1);
-    A.add(&s->scH, batched ? cap_high : 1);
     cudaError_t e = cudaMalloc(&s->arena, A.total());
     if (e != cudaSuccess) {
         tss_status st = e == cudaErrorMemoryAllocation ? TSS_OOM : TSS_CUDA_ERROR;
         delete s;
         return st;
     }
+    s->arena_bytes = A.total();
     A.carve(s->arena);
     s->L.g = grid_bufs_carve(gL, n_low > 0 ? n_low : 1, s->CL);
     s->H.g = grid_bufs_carve(gH, cap_high > 0 ? cap_high : 1, s->CH);
@@ -557,55 +423,29 @@ tss_status create_solver(const std::vector<SceneIn>& scenes, int cap_high, bool 
         return TSS_CUDA_ERROR;
     }
     cudaStream_t st = s->stream;
-    // host staging of the concatenated scenes
-    std::vector<float> lp(2 * static_cast<size_t>(n_low)), lv(2 * static_cast<size_t>(n_low), 0.0f);
-    std::vector<float> wp(2 * static_cast<size_t>(n_wall));
-    std::vector<uint16_t> ws(static_cast<size_t>(n_wall));
-    {
-        size_t ol = 0, ow = 0;
-        for (int k = 0; k < S; ++k) {
-            const SceneIn& sc = scenes[k];
-            std::memcpy(lp.data() + 2 * ol, sc.low_pos, sizeof(float) * 2 * sc.n_low);
-            if (sc.low_vel) std::memcpy(lv.data() + 2 * ol, sc.low_vel, sizeof(float) * 2 * sc.n_low);
-            std::memcpy(wp.data() + 2 * ow, sc.wall_pos, sizeof(float) * 2 * sc.n_wall);
-            for (int w = 0; w < sc.n_wall; ++w) ws[ow + w] = static_cast<uint16_t>(k);
-            ol += sc.n_low;
-            ow += sc.n_wall;
-        }
-    }
     // zero the whole arena: counts, maps (set to -1 below), pools
     e = cudaMemsetAsync(s->arena, 0, A.total(), st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s->d_table, s->h_table.data(), sizeof(Params) * S, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s->d_slot_base, s->h_slot_base.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && s->slotsL > 0)
-        k_fill_i32<<<particle_blocks(s->slotsL, 256), 256, 0, st>>>(s->L.map, s->slotsL, -1);
-    if (e == cudaSuccess && s->slotsH > 0)
-        k_fill_i32<<<particle_blocks(s->slotsH, 256), 256, 0, st>>>(s->H.map, s->slotsH, -1);
+    if (e == cudaSuccess) launch_fill_i32(s->L.map, s->slotsL, -1, st);
+    if (e == cudaSuccess) launch_fill_i32(s->H.map, s->slotsH, -1, st);
     if (e == cudaSuccess && n_low > 0) {
-        e = cudaMemcpyAsync(s->L.npos, lp.data(), sizeof(float2) * n_low, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(s->L.nvel, lv.data(), sizeof(float2) * n_low, cudaMemcpyHostToDevice, st);
-        k_iota<<<particle_blocks(n_low, 256), 256, 0, st>>>(s->L.nid, n_low);
+        e = cudaMemcpyAsync(s->L.npos, sc.low_pos, sizeof(float2) * n_low, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            if (sc.low_vel) e = cudaMemcpyAsync(s->L.nvel, sc.low_vel, sizeof(float2) * n_low, cudaMemcpyHostToDevice, st);
+        }
+        launch_iota(s->L.nid, n_low, st);
     }
-    k_set_counts<<<1, 1, 0, st>>>(s->cnt, n_low, 0);
+    launch_set_counts(s->cnt, n_low, 0, st);
     // boundary grid, once (initBoundaries, 3205-3238): iota ids, low grid
     if (e == cudaSuccess && n_wall > 0) {
-        e = cudaMemcpyAsync(wraw, wp.data(), sizeof(float2) * n_wall, cudaMemcpyHostToDevice, st);
-        k_iota<<<particle_blocks(n_wall, 256), 256, 0, st>>>(wid, n_wall);
+        e = cudaMemcpyAsync(wraw, sc.wall_pos, sizeof(float2) * n_wall, cudaMemcpyHostToDevice, st);
+        launch_iota(wid, n_wall, st);
         k_set_int<<<1, 1, 0, st>>>(nW_dev, n_wall);
         ReorderArgs a{};
         a.src_pos = wraw;
         a.dst_pos = s->wpos;
-        if (e == cudaSuccess && !batched) {
+        if (e == cudaSuccess)
             e = grid_build_enqueue(wraw, wid, nW_dev, n_wall, s->P.ox, s->P.oy, s->P.r, s->P.dimL[0], s->P.dimL[1],
                                    gw, a, &s->cnt->err, st);
-        } else if (e == cudaSuccess) {
-            e = cudaMemcpyAsync(wsc, ws.data(), sizeof(uint16_t) * n_wall, cudaMemcpyHostToDevice, st);
-            k_wall_keys<<<particle_blocks(n_wall, 256), 256, 0, st>>>(wraw, wsc, n_wall, s->d_table, gw);
-            if (e == cudaSuccess) e = grid_sort_enqueue(wid, nW_dev, n_wall, gw, a, &s->cnt->err, st);
-        }
     }
     if (e == cudaSuccess) e = s->prime_keys(st);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -627,25 +467,8 @@ tss_status tss_solver_create(const tss_config* cfg, int n_low, const float* low_
                              float mass_low, int cap_high, float mass_high, int n_wall, const float* wall_pos,
                              float mass_wall, tss_solver** out) {
     if (!out || !cfg) return TSS_INVALID_ARG;
-    std::vector<SceneIn> v{{cfg, n_low, low_pos, low_vel, mass_low, mass_high, n_wall, wall_pos, mass_wall}};
-    return create_solver(v, cap_high, false, out);
-}
-
-tss_status tss_batch_create(int n_scenes, const tss_scene_desc* scenes, int cap_high, tss_solver** out) {
-    if (!out || !scenes || n_scenes < 1) return TSS_INVALID_ARG;
-    std::vector<SceneIn> v;
-    for (int k = 0; k < n_scenes; ++k) {
-        const tss_scene_desc& d = scenes[k];
-        v.push_back({d.config, d.n_low, d.low_pos, d.low_vel, d.mass_low, d.mass_high, d.n_wall, d.wall_pos,
-                     d.mass_wall});
-    }
-    return create_solver(v, cap_high, true, out);
-}
-
-tss_status tss_solver_num_scenes(tss_solver* s, int* n) {
-    if (!s || !n) return TSS_INVALID_ARG;
-    *n = s->S;
-    return TSS_OK;
+    const SceneIn sc{cfg, n_low, low_pos, low_vel, mass_low, mass_high, n_wall, wall_pos, mass_wall};
+    return create_solver(sc, cap_high, out);
 }
 
 void tss_solver_destroy(tss_solver* s) { delete s; }
@@ -673,8 +496,11 @@ tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
         }
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
-    for (int k = 0; k < n_steps; ++k)
+    for (int k = 0; k < n_steps; ++k) {
         if ((e = cudaGraphLaunch(s->exec, st)) != cudaSuccess) return s->cuda_fail(e, "graph launch");
+        ++s->steps_issued;
+        s->phys_low = s->live_low;  // the step's grid build dropped the retired scenes' entries
+    }
     s->uploaded[0] = s->uploaded[1] = false;
     return TSS_OK;
 }
@@ -756,12 +582,20 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
     const int cap = scale == 0 ? s->nL : s->capH;
     const int slots = scale == 0 ? s->slotsL : s->slotsH;
     if (n < 0 || n > cap) return s->fail(TSS_INVALID_ARG, "count exceeds capacity");
-    if (scale == 0 && n != s->nL) return s->fail(TSS_INVALID_ARG, "the low-res count is fixed at creation");
+    const int64_t want_low = s->batched ? s->live_low : s->nL;
+    if (scale == 0 && n != want_low) return s->fail(TSS_INVALID_ARG, "the low-res count is fixed by the scenes");
     if (n > 0 && (!in->id || !in->pos || !in->state)) return s->fail(TSS_INVALID_ARG, "missing arrays");
     std::vector<char> seen(static_cast<size_t>(slots), 0);
     for (int i = 0; i < n; ++i) {
         const int id = in->id[i];
         if (id < 0 || id >= slots || seen[id]) return s->fail(TSS_INVALID_ARG, "ids must be unique and in range");
+        if (s->batched) {  // the slot must belong to an admitted scene
+            const int low = scale == 0 ? id : id >> 2;
+            const int sc = s->h_page_scene[static_cast<size_t>(low) >> 8];
+            const SceneRec& r = s->scenes[sc];
+            if (!r.live || low < r.sb || low >= r.sb + r.n_low)
+                return s->fail(TSS_INVALID_ARG, "id outside the admitted scenes");
+        }
         seen[id] = 1;
     }
     cudaError_t e = cudaDeviceSynchronize();
@@ -784,7 +618,7 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
         }
     }
     if (e == cudaSuccess && slots > 0) {
-        k_fill_i32<<<particle_blocks(slots, 256), 256, 0, s->stream>>>(b.map, slots, -1);
+        launch_fill_i32(b.map, slots, -1, s->stream);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -793,7 +627,8 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
         if (e == cudaSuccess) {
             int nL = scale == 0 ? n : c.cur[0];
             int nH = scale == 1 ? n : c.cur[1];
-            k_set_counts<<<1, 1, 0, s->stream>>>(s->cnt, nL, nH);
+            launch_set_counts(s->cnt, nL, nH, s->stream);
+            if (scale == 0) s->phys_low = n;
             e = s->prime_keys(s->stream);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         }
@@ -900,67 +735,6 @@ tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n) {
     for (int k = 0; k < TSS_NUM_STAGES && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&ms[k], s->ev[k], s->ev[k + 1]);
     if (e != cudaSuccess) return s->cuda_fail(e, "stage times");
     return TSS_OK;
-}
-
-tss_status tss_solver_scene_counts(tss_solver* s, int* n_low, int* n_high) {
-    if (!s) return TSS_INVALID_ARG;
-    tss_counts c;
-    tss_status st = tss_solver_counts(s, &c);
-    if (st != TSS_OK) return st;
-    if (n_low)
-        for (int k = 0; k < s->S; ++k) n_low[k] = s->h_slot_base[k + 1] - s->h_slot_base[k];
-    if (n_high) {
-        std::vector<int32_t> ids(static_cast<size_t>(c.n_high));
-        cudaError_t e = c.n_high ? cudaMemcpy(ids.data(), s->H.nid, sizeof(int32_t) * c.n_high, cudaMemcpyDeviceToHost)
-                                 : cudaSuccess;
-        if (e != cudaSuccess) return s->cuda_fail(e, "scene counts");
-        for (int k = 0; k < s->S; ++k) n_high[k] = 0;
-        for (int32_t id : ids) {
-            const int low = id >> 2;
-            const int k = static_cast<int>(std::upper_bound(s->h_slot_base.begin(), s->h_slot_base.end(), low) -
-                                           s->h_slot_base.begin()) - 1;
-            if (k >= 0 && k < s->S) ++n_high[k];
-        }
-    }
-    return TSS_OK;
-}
-
-tss_status tss_solver_download_scene(tss_solver* s, int scene, int scale, tss_scale_state* out) {
-    if (!s || !out || scene < 0 || scene >= s->S || (scale != 0 && scale != 1)) return TSS_INVALID_ARG;
-    tss_counts c;
-    tss_status st = tss_solver_counts(s, &c);
-    if (st != TSS_OK) return st;
-    const int n = scale == 0 ? c.n_low : c.n_high;
-    std::vector<int32_t> id(n);
-    std::vector<float> pos(2 * static_cast<size_t>(n)), vel(2 * static_cast<size_t>(n)), dens(n), pres(n);
-    std::vector<uint8_t> stt(n);
-    tss_scale_state all{n, id.data(), pos.data(), vel.data(), stt.data(), dens.data(), pres.data()};
-    if ((st = tss_solver_download(s, scale, &all)) != TSS_OK) return st;
-    const int shift = scale == 0 ? 0 : 2;
-    const int lo = s->h_slot_base[scene], hi = s->h_slot_base[scene + 1];
-    int m = 0;
-    for (int i = 0; i < n; ++i) {
-        const int low = id[i] >> shift;
-        if (low < lo || low >= hi) continue;
-        if (m < out->n) {
-            if (out->id) out->id[m] = id[i] - (lo << shift);
-            if (out->pos) {
-                out->pos[2 * m] = pos[2 * i];
-                out->pos[2 * m + 1] = pos[2 * i + 1];
-            }
-            if (out->vel) {
-                out->vel[2 * m] = vel[2 * i];
-                out->vel[2 * m + 1] = vel[2 * i + 1];
-            }
-            if (out->state) out->state[m] = stt[i];
-            if (out->dens) out->dens[m] = dens[i];
-            if (out->pres) out->pres[m] = pres[i];
-        }
-        ++m;
-    }
-    const bool fits = m <= out->n;
-    out->n = m;
-    return fits ? TSS_OK : s->fail(TSS_INVALID_ARG, "download buffer too small");
 }
 
 tss_status tss_solver_last_error(tss_solver* s, char* buf, int len) {

@@ -1,0 +1,176 @@
+// solver_impl.cuh -- the solver handle behind the C ABI (include/tss.h), shared by
+// solver.cu (single scenes and the calls common to every handle) and pool.cu
+// (pools and batches of scenes).
+//
+// Replaces WCSPHSolver + ParticleSystem's device storage (TwoScale2D/WCSPHSolver.cu:
+// 2287-3238, TwoScale2D/ParticleSystem.cpp:13-119).  Differences by design:
+//  * one device arena per solver, all state resident; no GL interop
+//  * the particle counts stay on the device (no per-step readback, 2760-2781);
+//    every kernel reads its count from device memory
+//  * a whole step is captured once into a CUDA graph and replayed
+//  * all handle state is per handle (the reference kept activeID in a function
+//    static, 2728)
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tss.h"
+#include "extent.hpp"
+#include "grid.cuh"
+#include "sph.cuh"
+
+namespace tss {
+
+struct ScaleBufs {
+    float2 *pos, *vel, *acc, *npos, *nvel;
+    uint8_t *st, *nst;
+    int32_t *id, *nid, *map;
+    float *dens, *pres, *q, *ndens, *npres;
+    GridBufs g;
+};
+
+inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Bump allocation of many arrays out of one cudaMalloc.
+struct Arena {
+    std::vector<std::pair<void**, size_t>> items;
+    template <class T>
+    void add(T** p, size_t count) { items.push_back({reinterpret_cast<void**>(p), al256(sizeof(T) * (count ? count : 1))}); }
+    size_t total() const {
+        size_t t = 0;
+        for (auto& it : items) t += it.second;
+        return t;
+    }
+    void carve(char* base) {
+        for (auto& it : items) {
+            *it.first = base;
+            base += it.second;
+        }
+    }
+};
+
+// One scene as the C ABI describes it.
+struct SceneIn {
+    const tss_config* cfg;
+    int n_low;
+    const float* low_pos;
+    const float* low_vel;
+    float mass_low, mass_high;
+    int n_wall;
+    const float* wall_pos;
+    float mass_wall;
+};
+
+// Where an admitted scene lives in a pool.
+struct SceneRec {
+    bool live = false;
+    int64_t sb = 0, n_low = 0;   // low-res slots [sb, sb + n_low); high-res slots 4x
+    int64_t cbL = 0, nCL = 0;    // low-res cells [cbL, cbL + nCL), nCL = grid cells + 1
+    int64_t cbH = 0, nCH = 0;    // high-res cells
+    int64_t wb = 0, nW = 0;      // wall particles
+    int64_t high_res = 0;        // high-res list entries reserved
+    int64_t admitted_step = 0;   // pool steps issued before the admission
+};
+
+bool valid_cfg(const tss_config* cfg);
+Params make_params(const SceneIn& sc);
+void scene_runs(const SceneIn& sc, tss_footprint* f);  // unrounded footprint
+
+// Host launchers of small kernels shared by the translation units.
+void launch_fill_i32(int32_t* p, int64_t n, int v, cudaStream_t s);
+void launch_iota(int32_t* p, int n, cudaStream_t s);
+void launch_set_counts(Counters* c, int nL, int nH, cudaStream_t s);
+void launch_keys_batched(const float2* pos, const int32_t* id, const int* n_ptr, int cap, const Params* table,
+                         const uint16_t* page_scene, int page_shift, int shift, int high, GridBufs g, cudaStream_t s);
+
+}  // namespace tss
+
+struct tss_solver {
+    tss_config cfg;
+    tss::Params P;               // a single scene's parameters; a pool's capacities
+    int nL = 0, capH = 0, slotsL = 0, slotsH = 0, nW = 0;
+    int CL = 0, CH = 0;
+    bool carry = false;
+    bool batched = false;        // a pool or batch of scenes
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    tss::ScaleBufs L{}, H{};
+    float2* wpos = nullptr;
+    int* woff = nullptr;
+    tss::Counters* cnt = nullptr;
+    uint8_t* split_flag = nullptr;
+    int32_t* split_ids = nullptr;
+    unsigned* split_tile = nullptr;
+    int split_ntiles = 1;
+    float2* relax_pos = nullptr;
+    float2* relax_vel = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int blocksL = 1, blocksH = 1;
+    bool uploaded[2] = {false, false};  // state replaced since the last step
+    bool profile = false;
+    cudaEvent_t ev[TSS_NUM_STAGES + 1] = {};
+    std::string err;
+
+    // ---- pools and batches ----
+    int S = 1;                           // scene table entries
+    std::vector<tss::Params> h_table;    // per-scene parameters (host copy)
+    tss::Params* d_table = nullptr;
+    uint16_t* scL = nullptr;             // scene of each sorted particle
+    uint16_t* scH = nullptr;
+    uint16_t* page_scene = nullptr;      // [slot pages] scene owning each page of low-res slots
+    std::vector<uint16_t> h_page_scene;
+    bool reserve_high = false;           // admissions reserve 4 high-res entries per low-res particle
+    tss::ExtentSet ex_slots, ex_cellsL, ex_cellsH, ex_walls;
+    int64_t high_reserved = 0;
+    std::vector<tss::SceneRec> scenes;   // by scene id
+    std::vector<int> free_ids;           // unused scene ids (a stack, lowest on top)
+    int n_live = 0;
+    int64_t live_low = 0;                // low-res particles of the admitted scenes
+    int64_t phys_low = 0;                // low-res list entries (retired ones stay until the next build)
+    int64_t steps_issued = 0;
+    int* usedL = nullptr;                // device ints: cells in use on each scale
+    int* usedH = nullptr;
+    int* wnum = nullptr;                 // device int: wall count of the scene being admitted
+    unsigned* ext_cnt = nullptr;         // device scratch of tss_pool_extract
+    tss::GridBufs gW{};                  // wall grid build scratch (per-scene views)
+    float2* wraw = nullptr;
+    int32_t* wid = nullptr;
+    int capW = 0;
+
+    tss_status fail(tss_status st, const std::string& msg) {
+        err = msg;
+        return st;
+    }
+    tss_status cuda_fail(cudaError_t e, const char* where) {
+        err = std::string(where) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? TSS_OOM : TSS_CUDA_ERROR;
+    }
+
+    tss::StepView view() const;
+    tss::ReorderArgs reorder_args(tss::ScaleBufs& b, bool high);
+    cudaError_t mark(int k, cudaStream_t s);
+    cudaError_t enqueue_step(cudaStream_t s);
+    cudaError_t prime_keys(cudaStream_t s);
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+
+    ~tss_solver() {
+        drop_graph();
+        for (auto& x : ev)
+            if (x) cudaEventDestroy(x);
+        if (stream) cudaStreamDestroy(stream);
+        if (arena) cudaFree(arena);
+    }
+};

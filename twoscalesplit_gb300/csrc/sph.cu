@@ -194,11 +194,12 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
                                            int cey, float rad, float Tle, float cB) {
     float2 accB = make_float2(0.f, 0.f);
     const int* woff = V.woff + P.cbL;
+    const float2* wpos = V.wpos + P.wb;
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimL[0];
         const int wb = woff[row + cex + 1];
         for (int k = woff[row + csx]; k < wb; ++k) {
-            const float2 pik = sub(p, V.wpos[k]);
+            const float2 pik = sub(p, wpos[k]);
             const float x = sq(pik);
             if (x > Tle) continue;  // NaN passes: the reference's 0 * NaN offset propagates it
             const float gm = wall_weight(sqrtf(x), rad, P.cs);
@@ -353,80 +354,84 @@ template <bool B>
 __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) {
     __shared__ unsigned s_warp[kSplitThreads / 32];
     __shared__ unsigned s_red[kSplitThreads / 32];
-    const int tile = blockIdx.x;
     const int n = V.cnt->cur[0];
     const int nH = V.cnt->cur[1];
-    const int ntiles = gridDim.x;
+    // tiles of the list in use, strided over the blocks (a pool's list is sized for
+    // its capacity); the last of them publishes the counts
+    const int ntiles = n > 0 ? (n + kSplitTile - 1) / kSplitTile : 1;
     const int capH = P0.capH;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned before = 0;
-    for (int t = threadIdx.x; t < tile; t += blockDim.x) before += V.split_tile[t];
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        unsigned before = 0;
+        for (int t = threadIdx.x; t < tile; t += blockDim.x) before += V.split_tile[t];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
-    if (lane == 0) s_red[warp] = before;
-    // warp-striped items: item k of lane l of warp w is tile base + (w*K + k)*32 + l,
-    // so each warp's ballots cover 32 consecutive particles in order
-    const int wbase = tile * kSplitTile + warp * kSplitItems * 32;
-    unsigned warp_count = 0;
-    unsigned masks[kSplitItems];
+        for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+        if (lane == 0) s_red[warp] = before;
+        // warp-striped items: item k of lane l of warp w is tile base + (w*K + k)*32 + l,
+        // so each warp's ballots cover 32 consecutive particles in order
+        const int wbase = tile * kSplitTile + warp * kSplitItems * 32;
+        unsigned warp_count = 0;
+        unsigned masks[kSplitItems];
 #pragma unroll
-    for (int k = 0; k < kSplitItems; ++k) {
-        const int i = wbase + k * 32 + lane;
-        const bool f = i < n && V.split_flag[i] != 0;
-        masks[k] = __ballot_sync(0xffffffffu, f);
-        warp_count += __popc(masks[k]);
-    }
-    if (lane == 0) s_warp[warp] = warp_count;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned w = lane < kSplitThreads / 32 ? s_warp[lane] : 0u;
-        unsigned r = lane < kSplitThreads / 32 ? s_red[lane] : 0u;
-        unsigned wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += t;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-        if (lane < kSplitThreads / 32) s_warp[lane] = wi - w + r;
-        const unsigned total = __shfl_sync(0xffffffffu, wi, kSplitThreads / 32 - 1) + r;
-        if (lane == 0 && tile == ntiles - 1) {
-            const int nsplit = static_cast<int>(total);
-            long long want = static_cast<long long>(nH) + 4LL * nsplit;
-            V.cnt->n_split = nsplit;
-            if (want > capH) {
-                atomicOr(&V.cnt->err, kErrCapacity);
-                want = nH + 4LL * ((capH - nH) / 4);
-            }
-            V.cnt->next[1] = static_cast<int>(want);
-            V.cnt->next[0] = n;
-        }
-    }
-    __syncthreads();
-    unsigned rank = s_warp[warp];
-    const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-    for (int k = 0; k < kSplitItems; ++k) {
-        const unsigned m = masks[k];
-        if (m & (1u << lane)) {
+        for (int k = 0; k < kSplitItems; ++k) {
             const int i = wbase + k * 32 + lane;
-            const unsigned r = rank + __popc(m & lt);
-            if (r < static_cast<unsigned>(n)) {
-                const int id = V.L.id[i];
-                V.split_ids[r] = id;
-                const long long hb = static_cast<long long>(nH) + 4LL * r;
-                if (hb + 4 <= capH) {
-                    if constexpr (B) {
-                        const Params P = V.table[V.scL[i]];
-                        make_children(P, V, i, id, hb);
-                    } else {
-                        make_children(P0, V, i, id, hb);
+            const bool f = i < n && V.split_flag[i] != 0;
+            masks[k] = __ballot_sync(0xffffffffu, f);
+            warp_count += __popc(masks[k]);
+        }
+        if (lane == 0) s_warp[warp] = warp_count;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = lane < kSplitThreads / 32 ? s_warp[lane] : 0u;
+            unsigned r = lane < kSplitThreads / 32 ? s_red[lane] : 0u;
+            unsigned wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+            if (lane < kSplitThreads / 32) s_warp[lane] = wi - w + r;
+            const unsigned total = __shfl_sync(0xffffffffu, wi, kSplitThreads / 32 - 1) + r;
+            if (lane == 0 && tile == ntiles - 1) {
+                const int nsplit = static_cast<int>(total);
+                long long want = static_cast<long long>(nH) + 4LL * nsplit;
+                V.cnt->n_split = nsplit;
+                if (want > capH) {
+                    atomicOr(&V.cnt->err, kErrCapacity);
+                    want = nH + 4LL * ((capH - nH) / 4);
+                }
+                V.cnt->next[1] = static_cast<int>(want);
+                V.cnt->next[0] = n;
+            }
+        }
+        __syncthreads();
+        unsigned rank = s_warp[warp];
+        const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+        for (int k = 0; k < kSplitItems; ++k) {
+            const unsigned m = masks[k];
+            if (m & (1u << lane)) {
+                const int i = wbase + k * 32 + lane;
+                const unsigned r = rank + __popc(m & lt);
+                if (r < static_cast<unsigned>(n)) {
+                    const int id = V.L.id[i];
+                    V.split_ids[r] = id;
+                    const long long hb = static_cast<long long>(nH) + 4LL * r;
+                    if (hb + 4 <= capH) {
+                        if constexpr (B) {
+                            const Params P = V.table[V.scL[i]];
+                            make_children(P, V, i, id, hb);
+                        } else {
+                            make_children(P0, V, i, id, hb);
+                        }
                     }
                 }
             }
+            rank += __popc(m);
         }
-        rank += __popc(m);
+        __syncthreads();  // s_warp / s_red are reused by the next tile
     }
 }
 
@@ -603,6 +608,7 @@ __device__ __forceinline__ void relax_force_one(const Params& P, const StepView&
     const int* offH = H.off + P.cbH;
     const int* offL = L.off + P.cbL;
     const int* woff = V.woff + P.cbL;
+    const float2* wpos = V.wpos + P.wb;
     float2 p = H.pos[i], v = H.vel[i];
     const float dens = H.dens[i], pre = H.pres[i];
     const float dens2 = dens * dens;
@@ -643,7 +649,7 @@ __device__ __forceinline__ void relax_force_one(const Params& P, const StepView&
         }
         const int wb = woff[row + cex + 1];
         for (int k = woff[row + csx]; k < wb; ++k) {
-            const float2 pik = sub(p, V.wpos[k]);
+            const float2 pik = sub(p, wpos[k]);
             const float gm = wall_weight(vnorm(pik), P.rh, P.cs);
             accB.x += P.cBH * gm * pik.x;
             accB.y += P.cBH * gm * pik.y;

@@ -34,7 +34,7 @@ struct ScaleView {
 
 struct StepView {
     ScaleView L, H;
-    const float2* wpos;     // walls in (low cell, id) order
+    const float2* wpos;     // walls: each scene's in (low cell, id) order from its wall base
     const int* woff;        // wall cell offsets on the low grid
     Counters* cnt;
     uint8_t* split_flag;    // [n_low]

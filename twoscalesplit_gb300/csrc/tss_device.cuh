@@ -32,8 +32,9 @@ struct Params {
     int capH;
     // scene placement in a batch (all zero for a single scene): cell bases of the
     // scene's low/high grids in the global cell space, its first low-res slot id,
-    // its low-res particle count and high-res cell count
-    int cbL, cbH, sbL, nLs, CHs;
+    // its low-res particle count, high-res cell count and first wall particle (the
+    // scene's wall cell offsets count from it)
+    int cbL, cbH, sbL, nLs, CHs, wb;
     // exact squared-distance cutoffs: x <= Tle_s  <=>  sqrtf(x) <= r_s and
     // x <= Tlt_s  <=>  sqrtf(x) < r_s, for x = dx*dx + dy*dy (IEEE sqrt is monotone
     // and correctly rounded, so these are the largest floats with that property)

@@ -219,6 +219,26 @@ def mixed_batch(n_scenes=512, seed=0, **kw):
     return [mixed_scene(rng, **kw) for _ in range(n_scenes)]
 
 
+def serving_trace(n_requests, rate_per_s, seed=0, n_min=1000, n_max=500000, h_min=200, h_max=5000):
+    """The serving workload: n_requests scene requests with Poisson arrivals at
+    rate_per_s, scenes as in mixed_scene with low-res counts log-uniform in
+    [n_min, n_max], horizons uniform in {h_min..h_max} steps.  Returns
+    [(scene, horizon, arrival_s)] in arrival order."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    for _ in range(n_requests):
+        t += rng.exponential(1.0 / rate_per_s)
+        sc = mixed_scene(rng, n_min=n_min, n_max=n_max)
+        out.append((sc, int(rng.integers(h_min, h_max + 1)), t))
+    return out
+
+
+def mean_work(n_min=1000, n_max=500000, h_min=200, h_max=5000):
+    """E[n_low * horizon] of serving_trace's distributions (independent draws):
+    the log-uniform mean (b - a) / ln(b / a) times the mean horizon."""
+    return (n_max - n_min) / math.log(n_max / n_min) * (h_min + h_max) / 2.0
+
+
 SCENES = {"dam_break_5k": dam_break_5k, "dam_break_1m": dam_break_1m}
 
 

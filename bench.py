@@ -418,6 +418,134 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """The serving workload: a stream of scene requests (counts log-uniform 1k-500k,
+    horizons 200-5000 steps) with Poisson arrivals at `--load` x the measured
+    capacity of the 512-scene batch (low-res particle-steps/s), served by the
+    library's serving loop over a pool sized from an HBM budget.  The same requests
+    are also run one at a time through the plain solver (create, horizon steps,
+    download of the final state), each timed; first-come-first-served completion
+    times of that single server follow from those service times and the same
+    arrivals.  A second, saturated run submits the first `--burst` requests at once
+    and compares its makespan with the plain solver's summed service times."""
+    import torch
+    from twoscalesplit_gb300 import _abi, build, scenes
+    from twoscalesplit_gb300.serving import (Request, Server, fifo_schedule, latency_summary, pool_bytes,
+                                             pool_config_for_budget)
+    from twoscalesplit_gb300.solver import Batch, Solver
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    # 1. capacity of the batched step on the 512-scene mixed batch
+    if args.capacity_lps:
+        cap_lps, cap_src = args.capacity_lps, "given on the command line"
+    else:
+        scs = scenes.mixed_batch(512, seed=0)
+        b = Batch(scs)
+        b.step(3)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.step(10)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        b.sync()
+        cap_lps = sum(sc.n_low for sc in scs) * 10 / (e0.elapsed_time(e1) / 1e3)
+        cap_src = "mixed_batch_512, 10 steps after 3 warm-up steps"
+        del b, scs
+    # 2. the request stream
+    rate = args.load * cap_lps / scenes.mean_work()
+    trace = scenes.serving_trace(args.requests, rate, seed=args.seed)
+    n_low = np.array([sc.n_low for sc, _, _ in trace], dtype=np.float64)
+    cells = np.array([sc.config.dims_low[0] * sc.config.dims_low[1] for sc, _, _ in trace], dtype=np.float64)
+    walls = np.array([sc.n_wall for sc, _, _ in trace], dtype=np.float64)
+    cfg = pool_config_for_budget(int(args.budget_gb * (1 << 30)), 1.25 * cells.sum() / n_low.sum() + 0.05,
+                                 1.25 * walls.sum() / n_low.sum() + 0.05, max_scenes=8192)
+    sv = Server(cfg, max_steps_per_launch=args.chunk, max_in_flight=2, staging_bytes=2 << 30)
+    # warm-up: graph capture, first-touch of the staging rings
+    warm = scenes.serving_trace(4, 1e3, seed=args.seed + 1, n_min=2000, n_max=20000, h_min=10, h_max=20)
+    sv.run([Request(sc, h, t) for sc, h, t in warm])
+    verify = sorted(range(len(trace)), key=lambda k: trace[k][0].n_low * trace[k][1])[:3]
+    reqs = [Request(sc, h, t, want_result=(k in verify)) for k, (sc, h, t) in enumerate(trace)]
+    clocks = ClockSampler(None)
+    clocks.start()
+    stats, summ, res = sv.run(reqs)
+    clk = clocks.stop()
+    lat = latency_summary(stats)
+    served = [k for k, st in enumerate(stats) if st["status"] in (_abi.TSS_OK, _abi.TSS_NUMERIC)]
+    numeric_served = sorted(k for k, st in enumerate(stats) if st["status"] == _abi.TSS_NUMERIC)
+    numeric_plain = []
+    # 3. the plain solver, one request at a time, each timed (create + steps + download)
+    service = np.zeros(len(trace))
+    exact = 0
+    plain_steps_ms = 0.0
+    for k, (sc, h, _) in enumerate(trace):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        sol = Solver.from_scene(sc)
+        sol.step(h)
+        lo, hi = sol.download(0), sol.download(1)
+        service[k] = time.perf_counter() - t0
+        if sol.counts()["error_bits"] & _abi.TSS_ERR_NUMERIC:
+            numeric_plain.append(k)
+        if k in verify and res[k] is not None:
+            same = True
+            for mine, theirs in ((lo, res[k][0]), (hi, res[k][1])):
+                a, b2 = np.argsort(mine["id"], kind="stable"), np.argsort(theirs["id"], kind="stable")
+                same &= all(np.array_equal(mine[f][a], theirs[f][b2]) for f in ("id", "pos", "vel", "state",
+                                                                               "dens", "pres"))
+            exact += int(same)
+        del sol
+    arrivals = np.array([t for _, _, t in trace])
+    plain_done = fifo_schedule(arrivals, service)
+    plain_lat = plain_done - arrivals
+    horizons = np.array([h for _, h, _ in trace], dtype=np.float64)
+    scene_steps = float(horizons[served].sum())
+    makespan = summ["makespan_s"] - float(arrivals.min())
+    plain_makespan = float(plain_done.max() - arrivals.min())
+    # 4. saturated: the first `burst` requests at once
+    nb = min(args.burst, len(trace))
+    st_b, summ_b, _ = sv.run([Request(sc, h, 0.0) for sc, h, _ in trace[:nb]])
+    burst_ss = float(sum(h for _, h, _ in trace[:nb]))
+    gpu_launches = int(summ["steps"] * 14 + len(served) * 16)
+    line = {"metric": "scene-steps/s", "value": scene_steps / makespan, "unit": "scene-steps/s", "n_gpus": 1,
+            "steps": int(summ["steps"]), "warmup": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"serving_{len(trace)}_poisson", "requests": len(trace),
+                       "arrival_rate_per_s": rate, "load": args.load,
+                       "capacity_low_particle_steps_per_s": cap_lps, "capacity_source": cap_src,
+                       "n_low": "log-uniform 1k-500k", "horizon": "uniform 200-5000",
+                       "hbm_budget_gb": args.budget_gb, "pool_bytes": pool_bytes(cfg),
+                       "pool": {"low_slots": cfg.low_slots, "high_particles": cfg.high_particles,
+                                "low_cells": cfg.low_cells, "high_cells": cfg.high_cells,
+                                "wall_particles": cfg.wall_particles},
+                       "max_steps_per_launch": args.chunk,
+                       "l2": "inputs of the steps are the pool state (no flush; served end to end)"},
+            "served": len(served), "rejected": int(sum(1 for st in stats if st["status"] == _abi.TSS_INVALID_ARG)),
+            "latency_s": lat, "low_particle_steps_per_s": float(n_low[served] @ horizons[served]) / makespan,
+            "mean_active_scenes": summ["mean_active"], "max_active_scenes": summ["max_active"],
+            "plain_one_at_a_time": {
+                "scene_steps_per_s": float(horizons.sum()) / plain_makespan,
+                "latency_s": {"p50_s": float(np.percentile(plain_lat, 50)), "p99_s": float(np.percentile(plain_lat, 99)),
+                              "mean_s": float(plain_lat.mean())},
+                "service_s_total": float(service.sum()),
+                "how": "each request timed through the plain solver (create, horizon steps, download); FIFO "
+                       "completion times from those service times and the same arrivals"},
+            "speedup_vs_plain": (scene_steps / makespan) / (float(horizons.sum()) / plain_makespan),
+            "saturated": {"requests": nb, "scene_steps_per_s": burst_ss / summ_b["makespan_s"],
+                          "plain_scene_steps_per_s": burst_ss / float(service[:nb].sum()),
+                          "speedup_vs_plain": float(service[:nb].sum()) / summ_b["makespan_s"],
+                          "mean_active_scenes": summ_b["mean_active"]},
+            "exact_vs_alone": f"{exact}/{len(verify)} requests bit-identical to the plain solver",
+            "non_finite": {"served": numeric_served, "plain": numeric_plain,
+                           "same_requests": numeric_served == numeric_plain},
+            "e2e": {"value": scene_steps / makespan, "unit": "scene-steps/s",
+                    "h2d_bytes_per_step": float(sum(16 * sc.n_low + 8 * sc.n_wall for sc, _, _ in trace)) / max(summ["steps"], 1),
+                    "d2h_bytes_per_step": float(sum(29 * 5 * sc.n_low for sc, _, _ in trace)) / max(summ["steps"], 1)},
+            "gpu_launches": gpu_launches, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -427,12 +555,21 @@ def main():
     ap.add_argument("--scene", default="dam_break_1m")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"])
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=400)
+    ap.add_argument("--load", type=float, default=0.8)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--chunk", type=int, default=8)
+    ap.add_argument("--burst", type=int, default=128)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--capacity-lps", type=float, default=0.0)
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

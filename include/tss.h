@@ -41,6 +41,19 @@ typedef enum tss_status {
  * tail of that list) and accumulates into the high-res sum, while the low-res
  * term stays zero.  Without the flag the term uses the low-res particles, as the
  * kernel's parameter list intends. */
+#define TSS_FLAG_TETHER_GUARD 0x4u
+/* TSS_FLAG_TETHER_GUARD: the tether (adjustPosition, WCSPHSolver.cu:1007-1022)
+ * scales the child-parent offset by lim / dist; a child that lands exactly on its
+ * parent (dist == 0) gets 0/0 = NaN there.  With the flag such a child keeps its
+ * position (the formula's limit: for dist below the tether radius it leaves the
+ * child where it is).  Off by default: the reference's arithmetic. */
+#define TSS_FLAG_MERGE 0x2u
+/* TSS_FLAG_MERGE: a split parent (low-res state 1) whose predicted position is
+ * outside the region of interest returns to state 0, and its four children are
+ * removed: they are marked state 2 ("deleted", WCSPHSolver.h:105) in that step's
+ * output and dropped by the next grid build.  The reference has no live removal
+ * (its stub, WCSPHSolver.cu:1053-1095, is under `if (false)`); this rule is this
+ * library's.  Mass m*#(low state 0) + m_high*#(high) is conserved exactly. */
 
 /* Solver parameters.  Mirrors WCSPHConfig (TwoScale2D/WCSPHSolver.h:14-35) plus the
  * constants the reference hard-codes (gravity 9.81: WCSPHSolver.cu:1805,2012; split
@@ -66,6 +79,8 @@ typedef struct tss_config {
                               /* (0 = the current reference tree, 4 = its older snapshot)   */
     float relax_dt_div;       /* relaxation sub-step = dt / relax_dt_div (10 in reference)  */
     unsigned flags;           /* TSS_FLAG_*                                                 */
+    float roi_velocity[2];    /* the ROI translates: at a scene's step k (from 0) it is     */
+                              /* roi + k * (roi_velocity * dt), in FP32; {0,0} = fixed      */
 } tss_config;
 
 /* Fill *cfg like WCSPHConfig::WCSPHConfig (TwoScale2D/WCSPHSolver.cu:2287-2332):
@@ -202,11 +217,14 @@ typedef struct tss_scene_result {
 
 /* Enqueue a copy of an admitted scene's state after its last step into `dst`,
  * whose arrays must be device-accessible (device memory or mapped page-locked
- * host memory) and 8-byte aligned; d_counts (2 device-accessible ints) receives
- * the particles of each scale.  Valid between a step and the next one, before
+ * host memory) and 8-byte aligned; d_counts (3 device-accessible ints) receives
+ * the particles of each scale and the number of them with a non-finite position,
+ * velocity or density (a scene that went unstable; the other scenes of the pool
+ * are not affected by it).  Valid between a step and the next one, before
  * the scene's retirement; cap[0] >= n_low and cap[1] >= 4 n_low always suffice.
  * Order within each scale: the list order (the last step's (cell, id) order,
- * then that step's new children). */
+ * then that step's new children); with TSS_FLAG_MERGE, children removed in the
+ * last step are included with state 2. */
 tss_status tss_pool_extract(tss_solver* s, int scene_id, const tss_scene_result* dst, int32_t* d_counts,
                             void* stream);
 
@@ -240,7 +258,8 @@ typedef struct tss_request_stats {
     double admit_s;             /* host time of the admission call */
     double done_s;              /* the final state is in host memory (GPU event time) */
     int64_t first_step;         /* pool step index of the scene's first step */
-    int32_t status;             /* TSS_OK, or TSS_INVALID_ARG if it can never fit */
+    int32_t status;             /* TSS_OK; TSS_NUMERIC: the final state has non-finite
+                                   particles; TSS_INVALID_ARG: it can never fit */
     int32_t n_low, n_high;      /* final counts */
 } tss_request_stats;
 
@@ -277,6 +296,7 @@ typedef struct tss_counts {
     int n_split_last;         /* parents split in the last step                       */
     long long steps;          /* steps taken                                          */
     unsigned error_bits;      /* device error word (TSS_ERR_*)                        */
+    int n_removed_last;       /* high-res particles removed by merges in the last step */
 } tss_counts;
 
 #define TSS_ERR_CAPACITY 0x1u /* a split would overflow the high-res pool            */

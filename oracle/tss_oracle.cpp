@@ -72,8 +72,11 @@ struct Consts {
     T cBL, cBH;  // wall mass ratios mB/(mL+mB), mB/(mH+mB)
     T relax_dt;
     T roi[4];
+    T roi_vdt[2];  // ROI displacement per step (roi_velocity * dt)
     int relax_iters;
     bool q1;
+    bool merge;    // TSS_FLAG_MERGE: split parents outside the ROI merge back
+    bool tether_guard;  // TSS_FLAG_TETHER_GUARD: no 0/0 when a child sits on its parent
 };
 
 // computeGridCoordinate(pos, offset), WCSPHSolver.cu:265-289.
@@ -204,6 +207,8 @@ public:
     std::vector<int32_t> fresh;  // low-res parents split last step
     std::vector<int32_t> split;  // parents split this step
     int overflow = 0;
+    long long steps_done = 0;    // the ROI of step k is roi + k * roi_vdt
+    int removed = 0;             // children removed by merges in the last step
 
     Oracle(const tss_config& c, float mL, float mH, float mB, int nL_slots, int cap_high,
            int n_wall, const float* wall_pos)
@@ -236,8 +241,12 @@ public:
         k.cBH = k.mB / (k.mH + k.mB);
         k.relax_dt = k.dt / T(c.relax_dt_div);
         for (int i = 0; i < 4; ++i) k.roi[i] = T(c.roi[i]);
+        k.roi_vdt[0] = T(c.roi_velocity[0]) * T(c.dt);
+        k.roi_vdt[1] = T(c.roi_velocity[1]) * T(c.dt);
         k.relax_iters = c.relax_iters;
         k.q1 = (c.flags & TSS_FLAG_Q1_COMPAT) != 0;
+        k.merge = (c.flags & TSS_FLAG_MERGE) != 0;
+        k.tether_guard = (c.flags & TSS_FLAG_TETHER_GUARD) != 0;
         slotsL = nL_slots;
         slotsH = 4 * nL_slots;
         capH = cap_high;
@@ -536,6 +545,10 @@ public:
         nxt_velL.resize(n);
         std::vector<uint8_t> flag(n, 0);
         const T hx = (k.r + k.rh) / T(2);
+        // the region of interest of this step (a rectangle moving by roi_vdt per step)
+        const T kf = T(steps_done);
+        const T rx0 = k.roi[0] + kf * k.roi_vdt[0], rx1 = k.roi[2] + kf * k.roi_vdt[0];
+        const T ry0 = k.roi[1] + kf * k.roi_vdt[1], ry1 = k.roi[3] + kf * k.roi_vdt[1];
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; ++i) {
             V2<T> p = L.s_pos[i], v = L.s_vel[i];
@@ -599,9 +612,12 @@ public:
             p.y += k.dt * v.y;
             nxt_posL[i] = p;
             nxt_velL[i] = v;
-            if (s == 0 && k.roi[0] < p.x && p.x < k.roi[2] && k.roi[1] < p.y && p.y < k.roi[3]) {
+            const bool in_roi = rx0 < p.x && p.x < rx1 && ry0 < p.y && p.y < ry1;
+            if (s == 0 && in_roi) {
                 nxt_stL[i] = 1;
                 flag[i] = 1;
+            } else if (k.merge && s == 1 && !in_roi) {
+                nxt_stL[i] = 0;  // merge back: the children are removed below
             }
         }
         split.clear();
@@ -688,8 +704,10 @@ public:
                 V2<T> pji{p.x - pl.x, p.y - pl.y};
                 T dist = norm2(pji);
                 T lim = T(std::fmin(double(dist), 0.75 * std::sqrt(double(k.mL) / (double(rho) * kPi))));
-                p.x = pl.x + lim / dist * pji.x;
-                p.y = pl.y + lim / dist * pji.y;
+                if (!(k.tether_guard && dist == T(0))) {
+                    p.x = pl.x + lim / dist * pji.x;
+                    p.y = pl.y + lim / dist * pji.y;
+                }
             }
             nxt_posH[i] = p;
             nxt_velH[i] = v;
@@ -721,11 +739,27 @@ public:
         L.st = nxt_stL;
         L.dens = L.s_dens;
         L.pres = L.s_pres;
-        // high: existing in sorted order, then 4 children per split (initSubParticlesAndAddToList)
-        std::vector<int32_t> hid = H.s_id;
-        std::vector<V2<T>> hpos = nxt_posH, hvel = nxt_velH;
-        std::vector<uint8_t> hst = H.s_st;
-        std::vector<T> hd = H.s_dens, hp = H.s_pres;
+        // high: existing in sorted order without the children of parents that merged
+        // back, then 4 children per split (initSubParticlesAndAddToList)
+        std::vector<int32_t> hid;
+        std::vector<V2<T>> hpos, hvel;
+        std::vector<uint8_t> hst;
+        std::vector<T> hd, hp;
+        removed = 0;
+        for (int i = 0; i < nH; ++i) {
+            const int parent = H.s_id[i] >> 2;
+            const int pi = (parent >= 0 && parent < slotsL) ? L.map[parent] : -1;
+            if (k.merge && pi >= 0 && L.s_st[pi] == 1 && nxt_stL[pi] == 0) {
+                ++removed;
+                continue;
+            }
+            hid.push_back(H.s_id[i]);
+            hpos.push_back(nxt_posH[i]);
+            hvel.push_back(nxt_velH[i]);
+            hst.push_back(H.s_st[i]);
+            hd.push_back(H.s_dens[i]);
+            hp.push_back(H.s_pres[i]);
+        }
         for (int q = 0; q < ns; ++q) {
             int i = split[q];
             int id = L.s_id[i];
@@ -752,6 +786,7 @@ public:
         H.pres.swap(hp);
         fresh = split_ids;
         split = split_ids;
+        ++steps_done;
         return TSS_OK;
     }
 };

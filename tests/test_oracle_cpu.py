@@ -251,3 +251,50 @@ def test_fp32_against_fp64_one_step():
         assert np.array_equal(o32.get(0, "sorted_id"), o64.get(0, "sorted_id"))
         d32, d64 = o32.get(0, "dens"), o64.get(0, "dens")
         assert np.max(np.abs(d32 - d64) / np.abs(d64)) < 1e-5
+
+
+def test_moving_roi_merge_conserves_mass_exactly():
+    """Builder-defined removal (TSS_FLAG_MERGE): split parents that leave the moving
+    region of interest merge back and their children are removed; the mass
+    m * #(low state 0) + m/4 * #(high) is conserved exactly (a count identity,
+    since m/4 is exact in FP32), in FP32 and FP64."""
+    from twoscalesplit_gb300 import scenes
+    for precision in (32, 64):
+        sc = scenes.adaptive_dam_break(30, 60, 0.4 / 30, roi_velocity=(16.0, 4.0), roi_start=(0.0, 0.05), steps=150)
+        orc = O.Oracle(sc, precision)
+        n = sc.n_low
+        seen_high, seen_merge = 0, 0
+        prev_transient = 0
+        for s in range(150):
+            orc.step()
+            st = orc.get(0, "state")
+            nh = orc.get(1, "id").shape[0]
+            assert 4 * int((st == 0).sum()) + nh == 4 * n, (precision, s)
+            assert nh == 4 * int((st == 1).sum())
+            seen_high = max(seen_high, nh)
+            seen_merge += int(prev_transient > (st == 1).sum())
+            prev_transient = int((st == 1).sum())
+        assert seen_high > 0 and seen_merge > 0
+
+
+def test_tether_guard_removes_the_zero_distance_nan():
+    """A mixed-workload droplet scene whose split children collapse onto their
+    parent: with the reference's tether a child landing exactly on the parent gets
+    0/0 = NaN; with TSS_FLAG_TETHER_GUARD it keeps its position and the scene stays
+    finite."""
+    import copy
+    from twoscalesplit_gb300 import scenes
+    sc0 = scenes.mixed_batch(47, seed=0)[46]
+    sc0.config.dt = np.float32(sc0.config.dt * 0.5)
+    finite = {}
+    for guard in (False, True):
+        sc = copy.deepcopy(sc0)
+        if guard:
+            sc.config.flags |= 0x4
+        else:
+            sc.config.flags &= ~0x4
+        orc = O.Oracle(sc, 32)
+        for _ in range(8):
+            orc.step()
+        finite[guard] = bool(np.isfinite(orc.get(1, "pos")).all())
+    assert finite == {False: False, True: True}

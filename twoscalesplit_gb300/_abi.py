@@ -25,6 +25,8 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "CAPACI
                 5: "NUMERIC", 6: "TIMEOUT", 7: "NO_DEVICE"}
 
 TSS_FLAG_Q1_COMPAT = 0x1
+TSS_FLAG_MERGE = 0x2
+TSS_FLAG_TETHER_GUARD = 0x4
 TSS_SCALE_LOW = 0
 TSS_SCALE_HIGH = 1
 
@@ -72,6 +74,7 @@ class TssConfig(ctypes.Structure):
         ("relax_iters", ctypes.c_int),
         ("relax_dt_div", ctypes.c_float),
         ("flags", ctypes.c_uint),
+        ("roi_velocity", ctypes.c_float * 2),
     ]
 
     def as_dict(self):
@@ -84,7 +87,8 @@ class TssConfig(ctypes.Structure):
 
 class TssCounts(ctypes.Structure):
     _fields_ = [("n_low", ctypes.c_int), ("n_high", ctypes.c_int), ("n_transient_low", ctypes.c_int),
-                ("n_split_last", ctypes.c_int), ("steps", ctypes.c_longlong), ("error_bits", ctypes.c_uint)]
+                ("n_split_last", ctypes.c_int), ("steps", ctypes.c_longlong), ("error_bits", ctypes.c_uint),
+                ("n_removed_last", ctypes.c_int)]
 
 
 class TssScaleState(ctypes.Structure):
@@ -189,6 +193,7 @@ def config_init(xs, ys, xe, ye, effective_radius, effective_radius_high, rest_de
     c.relax_iters = 0
     c.relax_dt_div = 10.0
     c.flags = TSS_FLAG_Q1_COMPAT
+    c.roi_velocity[:] = [0.0, 0.0]
     return c
 
 

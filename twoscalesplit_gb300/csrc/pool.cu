@@ -81,8 +81,9 @@ __global__ void k_retire(const int32_t* __restrict__ nid, const int* __restrict_
 // Split flags of the last step before the scene's first sorted low-res entry
 // (out[0]) and among its entries (out[1]).
 __global__ void k_count_splits(const uint8_t* __restrict__ flag, const int* __restrict__ offL, int cb, int ncells,
-                               const Counters* __restrict__ cnt, unsigned* out) {
+                               const Counters* __restrict__ cnt, unsigned* out, int32_t* d_counts) {
     const int lf = offL[cb], le = min(offL[cb + ncells], cnt->sorted[0]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) d_counts[2] = 0;  // k_extract counts non-finite particles into it
     unsigned a = 0, b = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < le; i += gridDim.x * blockDim.x) {
         const unsigned f = flag[i] != 0;
@@ -142,6 +143,9 @@ __global__ void k_extract(ExtractArgs a) {
             if (a.dst.state[0]) a.dst.state[0][t] = a.lst[k];
             if (a.dst.dens[0]) a.dst.dens[0][t] = a.ldens[k];
             if (a.dst.pres[0]) a.dst.pres[0][t] = a.lpres[k];
+            const float2 p = a.lpos[k], v = a.lvel[k];
+            if (!(isfinite(p.x) && isfinite(p.y) && isfinite(v.x) && isfinite(v.y) && isfinite(a.ldens[k])))
+                atomicAdd(&a.d_counts[2], 1);
         } else {
             const int j = static_cast<int>(tt - a.n_low);
             if (j >= ns + nk || j >= a.dst.cap[1]) continue;
@@ -155,6 +159,9 @@ __global__ void k_extract(ExtractArgs a) {
             const bool dv = !kid || a.kid_dens;
             if (a.dst.dens[1]) a.dst.dens[1][j] = dv ? a.hdens[k] : 0.0f;
             if (a.dst.pres[1]) a.dst.pres[1][j] = dv ? a.hpres[k] : 0.0f;
+            const float2 p = a.hpos[k], v = a.hvel[k];
+            if (!(isfinite(p.x) && isfinite(p.y) && isfinite(v.x) && isfinite(v.y) && (!dv || isfinite(a.hdens[k]))))
+                atomicAdd(&a.d_counts[2], 1);
         }
     }
 }
@@ -373,6 +380,7 @@ tss_status admit(tss_solver* s, const SceneIn& in, cudaStream_t st, int* scene_i
     P.slotsL = s->slotsL;
     P.slotsH = s->slotsH;
     P.capH = s->capH;
+    P.step0 = s->steps_issued;  // the scene's ROI motion starts at its first step
     s->h_table[id] = P;
     const int n = in.n_low, nW = in.n_wall;
     const int base = static_cast<int>(s->phys_low);
@@ -581,7 +589,7 @@ tss_status tss_pool_extract(tss_solver* s, int id, const tss_scene_result* dst, 
     cudaError_t e = cudaMemsetAsync(s->ext_cnt, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return s->cuda_fail(e, "extract");
     k_count_splits<<<particle_blocks(static_cast<int>(std::max<int64_t>(s->live_low, 1)), 256), 256, 0, st>>>(
-        s->split_flag, s->L.g.off, P.cbL, CLs, s->cnt, s->ext_cnt);
+        s->split_flag, s->L.g.off, P.cbL, CLs, s->cnt, s->ext_cnt, d_counts);
     ExtractArgs a{};
     a.sb = P.sbL;
     a.n_low = static_cast<int>(r.n_low);

@@ -211,7 +211,7 @@ struct Run {
             st.done_s = t;
             st.n_low = cnt[0];
             st.n_high = cnt[1];
-            st.status = TSS_OK;
+            st.status = cnt[2] == 0 ? TSS_OK : TSS_NUMERIC;
             last_done = std::max(last_done, t);
             ++served;
             tss_scene_result* out = reqs[f.req].result;
@@ -436,14 +436,19 @@ tss_status tss_server_run(tss_server* sv, int n, const tss_request* reqs, tss_re
         if (st != TSS_OK) break;
     }
     if (st == TSS_OK) st = R.drain();
-    if (st == TSS_OK) st = tss_solver_sync(sv->pool);
+    if (st == TSS_OK) {
+        // a scene that went unstable is that request's failure (TSS_NUMERIC in its
+        // stats); any other device error fails the run
+        st = tss_solver_sync(sv->pool);
+        if (st == TSS_NUMERIC) st = TSS_OK;
+    }
     if (summary) {
         summary->makespan_s = R.last_done;
         summary->steps = R.steps;
         int64_t ss = 0;
         double ps = 0;
         for (int i = 0; i < n; ++i)
-            if (stats[i].status == TSS_OK) {
+            if (stats[i].status == TSS_OK || stats[i].status == TSS_NUMERIC) {
                 ss += reqs[i].horizon;
                 ps += static_cast<double>(reqs[i].scene.n_low) * reqs[i].horizon;
             }

@@ -162,6 +162,7 @@ __global__ void k_set_counts(Counters* c, int nL, int nH) {
     c->cur[0] = c->next[0] = nL;
     c->cur[1] = c->next[1] = nH;
     c->h_state0 = 0;
+    c->n_drop = c->dropped = 0;
 }
 __global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
 
@@ -194,7 +195,7 @@ float sq_cutoff(float r, bool inclusive) {
 bool finite_cfg(const tss_config* c) {
     const float v[] = {c->domain_origin[0], c->domain_origin[1], c->domain_end[0], c->domain_end[1], c->r_low,
                        c->r_high, c->rest_density, c->tait_b, c->speed_sound, c->alpha, c->tension, c->dt,
-                       c->gravity, c->relax_dt_div};
+                       c->gravity, c->relax_dt_div, c->roi_velocity[0], c->roi_velocity[1]};
     for (float x : v)
         if (!std::isfinite(x)) return false;
     return true;
@@ -260,8 +261,13 @@ Params make_params(const SceneIn& sc) {
     P.hx = (cfg->r_low + cfg->r_high) / 2.0f;
     P.relax_dt = cfg->dt / cfg->relax_dt_div;
     for (int k = 0; k < 4; ++k) P.roi[k] = cfg->roi[k];
+    P.roi_vdt[0] = cfg->roi_velocity[0] * cfg->dt;  // FP32 products
+    P.roi_vdt[1] = cfg->roi_velocity[1] * cfg->dt;
     P.relax_iters = cfg->relax_iters;
     P.q1 = (cfg->flags & TSS_FLAG_Q1_COMPAT) ? 1 : 0;
+    P.merge = (cfg->flags & TSS_FLAG_MERGE) ? 1 : 0;
+    P.tether_guard = (cfg->flags & TSS_FLAG_TETHER_GUARD) ? 1 : 0;
+    P.step0 = 0;
     P.Tle_r = sq_cutoff(P.r, true);
     P.Tlt_r = sq_cutoff(P.r, false);
     P.Tle_rh = sq_cutoff(P.rh, true);
@@ -526,50 +532,92 @@ tss_status tss_solver_counts(tss_solver* s, tss_counts* out) {
     if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return s->cuda_fail(e, "counts");
     out->n_low = c.cur[0];
-    out->n_high = c.cur[1];
-    out->n_transient_low = c.cur[1] / 4;
+    out->n_high = c.cur[1] - c.dropped;  // removed entries wait in the list for the next build
+    out->n_transient_low = out->n_high / 4;
     out->n_split_last = c.n_split;
     out->steps = c.steps;
     out->error_bits = c.err;
+    out->n_removed_last = c.dropped;
     return TSS_OK;
 }
 
+namespace {
+
+// Copy the first np list entries of a scale into the given host arrays (any may be null).
+cudaError_t copy_list(tss_solver* s, int scale, int np, const tss_scale_state& o) {
+    ScaleBufs& b = scale == 0 ? s->L : s->H;
+    cudaError_t e = cudaSuccess;
+    if (np == 0) return e;
+    if (o.id) e = cudaMemcpy(o.id, b.nid, sizeof(int32_t) * np, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && o.pos) e = cudaMemcpy(o.pos, b.npos, sizeof(float2) * np, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && o.vel) e = cudaMemcpy(o.vel, b.nvel, sizeof(float2) * np, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && o.state) e = cudaMemcpy(o.state, b.nst, np, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && (o.dens || o.pres)) {
+        if (s->carry) {
+            if (o.dens) e = cudaMemcpy(o.dens, b.ndens, sizeof(float) * np, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && o.pres) e = cudaMemcpy(o.pres, b.npres, sizeof(float) * np, cudaMemcpyDeviceToHost);
+        } else {
+            // list order = last step's sorted order for the particles that existed then
+            Counters cc;
+            e = cudaMemcpy(&cc, s->cnt, sizeof(cc), cudaMemcpyDeviceToHost);
+            int m = (cc.steps > 0 && !s->uploaded[scale]) ? cc.sorted[scale] : 0;
+            if (m > np) m = np;
+            if (o.dens) {
+                std::memset(o.dens, 0, sizeof(float) * np);
+                if (e == cudaSuccess && m) e = cudaMemcpy(o.dens, b.dens, sizeof(float) * m, cudaMemcpyDeviceToHost);
+            }
+            if (o.pres) {
+                std::memset(o.pres, 0, sizeof(float) * np);
+                if (e == cudaSuccess && m) e = cudaMemcpy(o.pres, b.pres, sizeof(float) * m, cudaMemcpyDeviceToHost);
+            }
+        }
+    }
+    return e;
+}
+
+}  // namespace
+
+// The list of a scale; entries removed in the last step (state 2, still in the
+// list until the next grid build) are left out.
 tss_status tss_solver_download(tss_solver* s, int scale, tss_scale_state* out) {
     if (!s || !out || (scale != 0 && scale != 1)) return TSS_INVALID_ARG;
     tss_counts c;
     tss_status st = tss_solver_counts(s, &c);
     if (st != TSS_OK) return st;
     const int n = scale == 0 ? c.n_low : c.n_high;
-    ScaleBufs& b = scale == 0 ? s->L : s->H;
+    const int removed = scale == 1 ? c.n_removed_last : 0;
     if (out->n < n) {
         out->n = n;
         return s->fail(TSS_INVALID_ARG, "download buffer too small");
     }
     out->n = n;
-    if (n == 0) return TSS_OK;
-    cudaError_t e = cudaSuccess;
-    if (out->id) e = cudaMemcpy(out->id, b.nid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && out->pos) e = cudaMemcpy(out->pos, b.npos, sizeof(float2) * n, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && out->vel) e = cudaMemcpy(out->vel, b.nvel, sizeof(float2) * n, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && out->state) e = cudaMemcpy(out->state, b.nst, n, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && (out->dens || out->pres)) {
-        if (s->carry) {
-            if (out->dens) e = cudaMemcpy(out->dens, b.ndens, sizeof(float) * n, cudaMemcpyDeviceToHost);
-            if (e == cudaSuccess && out->pres) e = cudaMemcpy(out->pres, b.npres, sizeof(float) * n, cudaMemcpyDeviceToHost);
-        } else {
-            // list order = last step's sorted order for the particles that existed then
-            Counters cc;
-            e = cudaMemcpy(&cc, s->cnt, sizeof(cc), cudaMemcpyDeviceToHost);
-            int m = (cc.steps > 0 && !s->uploaded[scale]) ? cc.sorted[scale] : 0;
-            if (m > n) m = n;
-            if (out->dens) {
-                std::memset(out->dens, 0, sizeof(float) * n);
-                if (e == cudaSuccess && m) e = cudaMemcpy(out->dens, b.dens, sizeof(float) * m, cudaMemcpyDeviceToHost);
+    cudaError_t e;
+    if (removed == 0) {
+        e = copy_list(s, scale, n, *out);
+    } else {
+        const size_t np = static_cast<size_t>(n) + removed;
+        std::vector<int32_t> id(np);
+        std::vector<float> pos(2 * np), vel(2 * np), dens(np), pres(np);
+        std::vector<uint8_t> stt(np);
+        tss_scale_state t{static_cast<int>(np), id.data(), pos.data(), vel.data(), stt.data(), dens.data(), pres.data()};
+        e = copy_list(s, scale, static_cast<int>(np), t);
+        int m = 0;
+        for (size_t i = 0; i < np && e == cudaSuccess; ++i) {
+            if (stt[i] == 2) continue;
+            if (m >= n) break;
+            if (out->id) out->id[m] = id[i];
+            if (out->pos) {
+                out->pos[2 * m] = pos[2 * i];
+                out->pos[2 * m + 1] = pos[2 * i + 1];
             }
-            if (out->pres) {
-                std::memset(out->pres, 0, sizeof(float) * n);
-                if (e == cudaSuccess && m) e = cudaMemcpy(out->pres, b.pres, sizeof(float) * m, cudaMemcpyDeviceToHost);
+            if (out->vel) {
+                out->vel[2 * m] = vel[2 * i];
+                out->vel[2 * m + 1] = vel[2 * i + 1];
             }
+            if (out->state) out->state[m] = stt[i];
+            if (out->dens) out->dens[m] = dens[i];
+            if (out->pres) out->pres[m] = pres[i];
+            ++m;
         }
     }
     if (e != cudaSuccess) return s->cuda_fail(e, "download");

@@ -281,11 +281,20 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     L.nid[i] = L.id[i];
     grid_key(L.gcount, L.gkey, L.grank, L.gtile, i,
              P.cbL + cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
+    // split test on the predicted position (computeParticleAcceleration 1810-1835)
+    // against the ROI of this step; with TSS_FLAG_MERGE a split parent outside it
+    // merges back
+    const float kf = static_cast<float>(V.cnt->steps - P.step0);
+    const float rx0 = P.roi[0] + kf * P.roi_vdt[0], rx1 = P.roi[2] + kf * P.roi_vdt[0];
+    const float ry0 = P.roi[1] + kf * P.roi_vdt[1], ry1 = P.roi[3] + kf * P.roi_vdt[1];
+    const bool in_roi = rx0 < p.x && p.x < rx1 && ry0 < p.y && p.y < ry1;
     bool flag = false;
     uint8_t ns = static_cast<uint8_t>(s);
-    if (s == 0u && P.roi[0] < p.x && p.x < P.roi[2] && P.roi[1] < p.y && p.y < P.roi[3]) {
+    if (s == 0u && in_roi) {
         ns = 1;
         flag = true;
+    } else if (P.merge && s == 1u && !in_roi) {
+        ns = 0;
     }
     L.nst[i] = ns;
     V.split_flag[i] = flag ? 1 : 0;
@@ -502,27 +511,39 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     v.y += P.dt * acc.y;
     p.x += P.dt * v.x;
     p.y += P.dt * v.y;
-    // tether to the parent after the parent's advance (adjustPosition, 1007-1022)
+    // tether to the parent after the parent's advance (adjustPosition, 1007-1022);
+    // with TSS_FLAG_MERGE the children of a parent that merged back in this step
+    // are removed instead
     const int id = H.id[i];
     const int parent = id >> 2;
+    bool drop = false;
     if (parent >= 0 && parent < P.slotsL) {
         const int pi = L.map[parent];
-        if (pi >= 0 && L.st[pi] == 1) {
+        drop = P.merge && pi >= 0 && L.st[pi] == 1 && L.nst[pi] == 0;
+        if (pi >= 0 && L.st[pi] == 1 && !drop) {
             const float2 pl = L.npos[pi];
             const float rho = L.dens[pi];
             const float2 pji = sub(p, pl);
             const float dist = vnorm(pji);
             const float lim = static_cast<float>(fmin(
                 static_cast<double>(dist), 0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(rho) * kPi))));
-            p.x = pl.x + lim / dist * pji.x;
-            p.y = pl.y + lim / dist * pji.y;
+            if (!(P.tether_guard && dist == 0.0f)) {  // guarded: a child on its parent stays there
+                p.x = pl.x + lim / dist * pji.x;
+                p.y = pl.y + lim / dist * pji.y;
+            }
         }
     }
     H.npos[i] = p;
     H.nvel[i] = v;
-    H.nst[i] = static_cast<uint8_t>(s);
+    H.nst[i] = static_cast<uint8_t>(drop ? 2u : s);
     H.nid[i] = id;
-    grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, P.cbH + cell_hash(p, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
+    if (drop) {  // out of the next grid build, and of the slot map
+        H.gkey[i] = -1;
+        H.map[id] = -1;
+        atomicAdd(&V.cnt->n_drop, 1);
+    } else {
+        grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, P.cbH + cell_hash(p, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
+    }
     if (H.ndens) {
         H.ndens[i] = dens;
         H.npres[i] = H.pres[i];
@@ -705,6 +726,8 @@ __global__ void k_step_finish(Counters* c) {
         c->n_fresh = c->n_split;
         c->h_state0 = 0;
         c->steps += 1;
+        c->dropped = c->n_drop;
+        c->n_drop = 0;
     }
 }
 

@@ -26,8 +26,12 @@ struct Params {
     float hx;              // (r + rh) / 2, the cross-scale viscosity length
     float relax_dt;
     float roi[4];
+    float roi_vdt[2];      // ROI displacement per step (roi_velocity * dt)
     int relax_iters;
     int q1;
+    int merge;             // TSS_FLAG_MERGE
+    int tether_guard;      // TSS_FLAG_TETHER_GUARD
+    long long step0;       // the step counter when the scene started (its ROI's step 0)
     int slotsL, slotsH;    // slot-id spaces: low ids < slotsL, high ids < slotsH = 4*slotsL
     int capH;
     // scene placement in a batch (all zero for a single scene): cell bases of the
@@ -52,6 +56,8 @@ struct Counters {
     int h_state0;    // 1 if some high-res particle has (state & 1) == 0
     long long steps;
     int sorted[2];   // particles sorted in the last step (its `cur` counts)
+    int n_drop;      // high-res list entries removed (state 2) in this step
+    int dropped;     // ... in the last step: they are still in the list until the next build
 };
 
 __device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating

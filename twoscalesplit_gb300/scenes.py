@@ -37,7 +37,7 @@ import math
 
 import numpy as np
 
-from ._abi import TssConfig, config_init
+from ._abi import TSS_FLAG_MERGE, TSS_FLAG_TETHER_GUARD, TssConfig, config_init
 
 REST_DENSITY = 1000.0
 GAMMA = 7
@@ -150,6 +150,29 @@ def dam_break_1m(seed=0, relax_iters=0, **kw):
                       4_000_000, relax_iters, seed, **kw)
 
 
+def adaptive_dam_break(nx, ny, dx, roi_size=0.3, roi_start=(0.05, 0.05), roi_velocity=(0.5, 0.0), steps=2000,
+                       seed=0, cap_high=None, relax_iters=0, flags=None):
+    """A dam break filling [0, nx*dx]x[0, ny*dx] whose region of interest (a square
+    of side roi_size, lower-left corner roi_start) translates at roi_velocity units
+    per second, with TSS_FLAG_MERGE: particles split as the region reaches them and
+    merge back as it leaves them.  dt at dam_break_5k's Courant number; the tether
+    guard on (TSS_FLAG_TETHER_GUARD)."""
+    dt = 1e-4 * dx / 0.008
+    roi = [roi_start[0], roi_start[1], roi_start[0] + roi_size, roi_start[1] + roi_size]
+    sc = _dam_break(f"adaptive_dam_break_{nx}x{ny}", nx, ny, dx, roi, dt, steps,
+                    cap_high if cap_high is not None else 4 * nx * ny, relax_iters, seed, flags=flags)
+    sc.config.roi_velocity[:] = list(roi_velocity)
+    sc.config.flags |= TSS_FLAG_MERGE | TSS_FLAG_TETHER_GUARD
+    return sc
+
+
+def adaptive_8m(seed=0, **kw):
+    """The adaptive stress workload: 2000x4000 lattice at spacing 2e-4 (8M low-res
+    particles), a 0.3x0.3 region of interest translating at 0.5 units/s, high-res
+    pool of 32M, 2000 steps."""
+    return adaptive_dam_break(2000, 4000, 2e-4, cap_high=32_000_000, seed=seed, **kw)
+
+
 def dam_break_small(nx, ny, dx=None, seed=0, roi=None, relax_iters=4, cap_high=None, **kw):
     """A dam break of any lattice size filling [0,0.4]x[0,0.8] (test cases)."""
     if dx is None:
@@ -173,6 +196,11 @@ def _box_scene(name, fluid, dx, roi, steps, cap_factor, seed_rng, relax_iters=0,
                       REST_DENSITY, TAIT_B, SPEED_SOUND, ALPHA, SIGMA, 1e-4 * dx / 0.008)
     cfg.roi[:] = roi
     cfg.relax_iters = relax_iters
+    # The four children of a split start below rest density, attract, and can land
+    # exactly on their parent, where the reference's tether divides 0 by 0: without
+    # the guard about a third of the large scenes with large regions of interest go
+    # non-finite within a few thousand steps (the oracle agrees bit for bit).
+    cfg.flags |= TSS_FLAG_TETHER_GUARD
     m = REST_DENSITY * dx * dx
     if calibrate_mass:
         m = REST_DENSITY / lattice_pair_kernel_sum(dx, float(cfg.r_low), float(cfg.r_high))
@@ -188,7 +216,8 @@ def mixed_scene(rng, n_min=2000, n_max=200000, steps=1000, cap_factor=4.0):
     U[0.5,0.8]) above a pool of depth U[0.1,0.4]; low-res count log-uniform in
     [n_min, n_max]; spacing from the count and the fluid area; the region of
     interest a rectangle covering U[10%,40%] of the box at a uniform position; dt
-    at the Courant number of dam_break_5k; mass calibrated to rest density."""
+    at the Courant number of dam_break_5k; mass calibrated to rest density; the
+    tether guard on (TSS_FLAG_TETHER_GUARD)."""
     n_target = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
     if rng.uniform() < 0.5:
         w, h = rng.uniform(0.2, 0.5), rng.uniform(0.4, 0.9)
@@ -239,7 +268,7 @@ def mean_work(n_min=1000, n_max=500000, h_min=200, h_max=5000):
     return (n_max - n_min) / math.log(n_max / n_min) * (h_min + h_max) / 2.0
 
 
-SCENES = {"dam_break_5k": dam_break_5k, "dam_break_1m": dam_break_1m}
+SCENES = {"dam_break_5k": dam_break_5k, "dam_break_1m": dam_break_1m, "adaptive_8m": adaptive_8m}
 
 
 def make_scene(name, seed=0, **kw):

@@ -133,7 +133,7 @@ class Pool(Batch):
             res.cap[k] = caps[k]
             for name in ("id", "pos", "vel", "state", "dens", "pres"):
                 getattr(res, name)[k] = b[name].data_ptr()
-        counts = torch.zeros(2, dtype=torch.int32, device=dev)
+        counts = torch.zeros(3, dtype=torch.int32, device=dev)
         s = stream if stream else torch.cuda.current_stream().cuda_stream
         self._check(self.lib.tss_pool_extract(self.h, int(sid), ctypes.byref(res), ctypes.c_void_p(counts.data_ptr()),
                                               ctypes.c_void_p(s)))
@@ -224,8 +224,9 @@ class Server:
 
 
 def latency_summary(stats):
-    """p50/p99/mean completion latency (done - arrival) of the served requests."""
-    lat = np.array([s["done_s"] - s["arrival_s"] for s in stats if s["status"] == _abi.TSS_OK])
+    """p50/p99/mean completion latency (done - arrival) of the served requests
+    (those that completed, including any whose scene went non-finite)."""
+    lat = np.array([s["done_s"] - s["arrival_s"] for s in stats if s["status"] in (_abi.TSS_OK, _abi.TSS_NUMERIC)])
     if lat.size == 0:
         return {"p50_s": None, "p99_s": None, "mean_s": None, "served": 0}
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),

@@ -396,6 +396,37 @@ tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, int n,
                           int dimx, int dimy, int32_t* d_order, int32_t* d_cell_off,
                           void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Headless rendering                                                            */
+/* ------------------------------------------------------------------------- */
+/* Particle splats into a device RGBA image (4 floats per pixel, row 0 at the
+ * bottom), the reference's display() without OpenGL (TwoScale2D/main.cpp:65-102;
+ * QuantityRenderer/PointRenderer and their shaders): each particle is a disc of
+ * radius point_size in normalised device coordinates around
+ * ((p - xs) / (xe - xs) * 2 - 1, (p - ys) / (ye - ys) * 2 - 1), coloured by the jet
+ * map of min(|rho - rho0|, 400) / 400 or by a constant colour, alpha 0.5, blended
+ * as dst = 0.5 src + 0.5 dst in particle order.  A pixel is covered when its
+ * centre lies in the disc. */
+typedef struct tss_view {
+    float xs, ys, xe, ye;   /* display rectangle (scene units) */
+    int width, height;      /* image size in pixels (the reference's window: 1100 x 1100) */
+} tss_view;
+tss_status tss_render_workspace_size(int n, const tss_view* view, float point_size, size_t* bytes);
+/* Fill with the clear colour (1, 1, 1, 0) (main.cpp:73-74). */
+tss_status tss_render_clear(float* d_rgba, int width, int height, void* stream);
+/* Splat n particles (d_pos: 2 floats each).  d_dens non-NULL: jet colour of the
+ * visual quantity; NULL: the colour rgb[3]. */
+tss_status tss_render_splats(const tss_view* view, int n, const float* d_pos, const float* d_dens,
+                             float rest_density, const float* rgb, float point_size, float* d_rgba,
+                             void* d_workspace, size_t workspace_bytes, void* stream);
+/* One frame of a single-scene solver: clear, low-res (jet, point_sizes[0]), high-res
+ * (jet, point_sizes[1]), walls (black, point_sizes[2]); the reference drew with
+ * 0.005, 0.003 and 0.005 (main.cpp:176-190).  Densities are the last step's (the
+ * children created in it count as 0).  The first call allocates the solver's
+ * render scratch. */
+tss_status tss_solver_render(tss_solver* s, const tss_view* view, const float* point_sizes, float* d_rgba,
+                             void* stream);
+
 /* Grid build that allocates nothing.  No counterpart in the reference: it is
  * tss_grid_build with its scratch in a fixed array inside this library, for callers
  * that may not call cudaMalloc/cudaFree (a host application's per-frame callback,

@@ -31,6 +31,8 @@ def _orc_lib():
         lib.orc_destroy.argtypes = [vp]
         lib.orc_set_scale.argtypes = [vp, i, i, vp, vp, vp, vp, vp, vp]
         lib.orc_set_fresh.argtypes = [vp, i, vp]
+        lib.orc_set_steps.argtypes = [vp, ctypes.c_longlong]
+        lib.orc_splat.argtypes = [vp, i, i, i, vp, vp, i, f, vp, f, vp]
         lib.orc_step.argtypes = [vp]
         lib.orc_get.argtypes = [vp, i, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         lib.orc_set_threads.argtypes = [i]
@@ -95,6 +97,26 @@ def grid(pos, ids, origin, cell, dims):
     return order, off
 
 
+def splat(view, width, height, pos, dens=None, nvalid=None, rest_density=1000.0, rgb=None, point_size=0.005,
+          img=None):
+    """The CPU restatement of the headless splat renderer: blends the particles, in
+    order, into img (height x width x 4 float32, row 0 at the bottom; a new image
+    cleared to (1, 1, 1, 0) when None) and returns it."""
+    lib = _orc_lib()
+    if img is None:
+        img = np.zeros((height, width, 4), np.float32)
+        img[..., :3] = 1.0
+    img = np.ascontiguousarray(img, np.float32)
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 2)
+    n = pos.shape[0]
+    v = np.asarray(view, np.float32)
+    d = None if dens is None else np.ascontiguousarray(dens, np.float32)
+    c = None if rgb is None else np.asarray(rgb, np.float32)
+    lib.orc_splat(_p(v), width, height, n, _p(pos), _p(d), n if nvalid is None else int(nvalid),
+                  float(rest_density), _p(c), float(point_size), _p(img))
+    return img
+
+
 class Oracle:
     """One scene in the CPU oracle.  State arrays are in list order."""
 
@@ -130,6 +152,10 @@ class Oracle:
     def set_fresh(self, parents):
         parents = np.ascontiguousarray(parents, np.int32)
         self.lib.orc_set_fresh(self.h, parents.shape[0], _p(parents))
+
+    def set_steps(self, steps):
+        """Steps taken so far (the moving region of interest's step index)."""
+        self.lib.orc_set_steps(self.h, int(steps))
 
     def step(self):
         return self.lib.orc_step(self.h)

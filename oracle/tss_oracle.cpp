@@ -905,6 +905,63 @@ int orc_set_fresh(void* p, int n, const int32_t* parents) {
     return TSS_OK;
 }
 
+// Headless splat renderer restated on the CPU (the reference's display():
+// TwoScale2D/main.cpp:65-102 with QuantityRenderer/PointRenderer and their
+// shaders): each particle, in order, blends every pixel whose centre lies in its
+// disc; same FP32 expressions as the GPU rasterizer.  view = {xs, ys, xe, ye};
+// img holds W*H RGBA floats (row 0 at the bottom) and is blended into.
+int orc_splat(const float* view, int W, int H, int n, const float* pos, const float* dens, int nvalid, float rho0,
+              const float* rgb, float ps, float* img) {
+    const float xs = view[0], ys = view[1], w = view[2] - view[0], h = view[3] - view[1];
+    auto clamp01 = [](float v) { return std::fmin(std::fmax(v, 0.0f), 1.0f); };
+    for (int i = 0; i < n; ++i) {
+        const float cx = (pos[2 * i] - xs) / w * 2.0f - 1.0f;
+        const float cy = (pos[2 * i + 1] - ys) / h * 2.0f - 1.0f;
+        const float fx0 = (cx - ps + 1.0f) * 0.5f * W - 0.5f, fx1 = (cx + ps + 1.0f) * 0.5f * W - 0.5f;
+        const float fy0 = (cy - ps + 1.0f) * 0.5f * H - 0.5f, fy1 = (cy + ps + 1.0f) * 0.5f * H - 0.5f;
+        if (!(fx1 >= -1.0f && fx0 <= W && fy1 >= -1.0f && fy0 <= H)) continue;
+        const int x0 = std::max(0, (int)std::floor(std::fmax(fx0, -2.0f)) - 1);
+        const int x1 = std::min(W - 1, (int)std::ceil(std::fmin(fx1, W + 2.0f)) + 1);
+        const int y0 = std::max(0, (int)std::floor(std::fmax(fy0, -2.0f)) - 1);
+        const int y1 = std::min(H - 1, (int)std::ceil(std::fmin(fy1, H + 2.0f)) + 1);
+        float col[3];
+        if (dens) {  // jet colour of min(|rho - rho0|, 400) / 400
+            const float rho = i < nvalid ? dens[i] : 0.0f;
+            const float f = 4.0f * (std::fmin(std::fabs(rho - rho0), 400.0f) / 400.0f);
+            col[0] = clamp01(std::fmin(f - 1.5f, -f + 4.5f));
+            col[1] = clamp01(std::fmin(f - 0.5f, -f + 3.5f));
+            col[2] = clamp01(std::fmin(f + 0.5f, -f + 2.5f));
+        } else {
+            col[0] = rgb[0];
+            col[1] = rgb[1];
+            col[2] = rgb[2];
+        }
+        for (int py = y0; py <= y1; ++py) {
+            const float yp = ((float)py + 0.5f) / (float)H * 2.0f - 1.0f;
+            for (int px = x0; px <= x1; ++px) {
+                const float xp = ((float)px + 0.5f) / (float)W * 2.0f - 1.0f;
+                const float rx = (xp - cx) / ps, ry = (yp - cy) / ps;
+                if (rx * rx + ry * ry <= 1.0f) {
+                    float* c = img + 4 * ((size_t)py * W + px);
+                    c[0] = 0.5f * col[0] + 0.5f * c[0];
+                    c[1] = 0.5f * col[1] + 0.5f * c[1];
+                    c[2] = 0.5f * col[2] + 0.5f * c[2];
+                    c[3] = 0.5f * 0.5f + 0.5f * c[3];
+                }
+            }
+        }
+    }
+    return TSS_OK;
+}
+
+// Steps taken (the moving region of interest's step index), e.g. after loading a
+// state taken from a solver after that many steps.
+int orc_set_steps(void* p, long long steps) {
+    Handle* h = (Handle*)p;
+    if (h->f) h->f->steps_done = steps; else h->d->steps_done = steps;
+    return TSS_OK;
+}
+
 int orc_step(void* p) {
     Handle* h = (Handle*)p;
     return h->f ? h->f->step() : h->d->step();

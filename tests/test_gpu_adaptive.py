@@ -24,8 +24,8 @@ def _built():
 def test_moving_roi_merge_matches_oracle_and_conserves_mass(relax, q1):
     sc = scenes.adaptive_dam_break(40, 80, 0.01, roi_velocity=(20.0, 5.0), roi_start=(0.0, 0.05), steps=240,
                                    relax_iters=relax)
-    if not q1:
-        sc.config.flags &= ~1
+    if q1:
+        sc.config.flags |= 1  # the reference's high-res density term (TSS_FLAG_Q1_COMPAT)
     sol = Solver.from_scene(sc)
     orc = O.Oracle(sc, 32)
     n = sc.n_low

@@ -158,6 +158,12 @@ class TssServeSummary(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class TssView(ctypes.Structure):
+    """struct tss_view: display rectangle and image size."""
+    _fields_ = [("xs", ctypes.c_float), ("ys", ctypes.c_float), ("xe", ctypes.c_float), ("ye", ctypes.c_float),
+                ("width", ctypes.c_int), ("height", ctypes.c_int)]
+
+
 class TssBuffers(ctypes.Structure):
     _fields_ = [("pos", ctypes.c_void_p * 2), ("vel", ctypes.c_void_p * 2), ("dens", ctypes.c_void_p * 2),
                 ("id", ctypes.c_void_p * 2), ("state", ctypes.c_void_p * 2), ("counts", ctypes.c_void_p)]
@@ -251,6 +257,10 @@ def load_library(path=None):
         "tss_server_run": (i, [vp, i, ctypes.POINTER(TssRequest), ctypes.POINTER(TssRequestStats),
                                ctypes.POINTER(TssServeSummary)]),
         "tss_server_destroy": (None, [vp]),
+        "tss_render_workspace_size": (i, [i, ctypes.POINTER(TssView), f, ctypes.POINTER(ctypes.c_size_t)]),
+        "tss_render_clear": (i, [vp, i, i, vp]),
+        "tss_render_splats": (i, [ctypes.POINTER(TssView), i, vp, vp, f, fp, f, vp, vp, ctypes.c_size_t, vp]),
+        "tss_solver_render": (i, [vp, ctypes.POINTER(TssView), fp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

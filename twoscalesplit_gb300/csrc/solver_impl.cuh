@@ -143,6 +143,8 @@ struct tss_solver {
     float2* wraw = nullptr;
     int32_t* wid = nullptr;
     int capW = 0;
+    void* render_ws = nullptr;           // tss_solver_render scratch, allocated at its first call
+    size_t render_ws_bytes = 0;
 
     tss_status fail(tss_status st, const std::string& msg) {
         err = msg;
@@ -172,5 +174,6 @@ struct tss_solver {
             if (x) cudaEventDestroy(x);
         if (stream) cudaStreamDestroy(stream);
         if (arena) cudaFree(arena);
+        if (render_ws) cudaFree(render_ws);
     }
 };

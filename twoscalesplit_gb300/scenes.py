@@ -156,11 +156,15 @@ def adaptive_dam_break(nx, ny, dx, roi_size=0.3, roi_start=(0.05, 0.05), roi_vel
     of side roi_size, lower-left corner roi_start) translates at roi_velocity units
     per second, with TSS_FLAG_MERGE: particles split as the region reaches them and
     merge back as it leaves them.  dt at dam_break_5k's Courant number; the tether
-    guard on (TSS_FLAG_TETHER_GUARD)."""
+    guard on (TSS_FLAG_TETHER_GUARD) and the Q1 compatibility path off (its term
+    depends on the sorted order of the high-res list, so an FP64 evaluation of the
+    same state, whose cell hashing may order a boundary particle differently, is not
+    comparable with it)."""
     dt = 1e-4 * dx / 0.008
     roi = [roi_start[0], roi_start[1], roi_start[0] + roi_size, roi_start[1] + roi_size]
     sc = _dam_break(f"adaptive_dam_break_{nx}x{ny}", nx, ny, dx, roi, dt, steps,
-                    cap_high if cap_high is not None else 4 * nx * ny, relax_iters, seed, flags=flags)
+                    cap_high if cap_high is not None else 4 * nx * ny, relax_iters, seed,
+                    flags=0 if flags is None else flags)
     sc.config.roi_velocity[:] = list(roi_velocity)
     sc.config.flags |= TSS_FLAG_MERGE | TSS_FLAG_TETHER_GUARD
     return sc

@@ -123,6 +123,18 @@ class Solver:
         self._check(self.lib.tss_solver_stage_times(self.h, fptr(ms), ms.shape[0]))
         return dict(zip(_abi.STAGE_NAMES, ms.tolist()))
 
+    def render(self, view, point_sizes=(0.005, 0.003, 0.005), stream=None):
+        """One frame (tss_solver_render): a torch CUDA tensor (height, width, 4),
+        row 0 at the bottom.  `view` is (xs, ys, xe, ye, width, height)."""
+        import torch
+        v = _abi.TssView(*[float(x) for x in view[:4]], int(view[4]), int(view[5]))
+        img = torch.empty((v.height, v.width, 4), dtype=torch.float32, device="cuda")
+        ps = np.asarray(point_sizes, np.float32)
+        s = stream if stream else torch.cuda.current_stream().cuda_stream
+        self._check(self.lib.tss_solver_render(self.h, ctypes.byref(v), fptr(ps), ctypes.c_void_p(img.data_ptr()),
+                                               ctypes.c_void_p(s)))
+        return img
+
     def device_buffers(self):
         b = TssBuffers()
         self._check(self.lib.tss_solver_device_buffers(self.h, ctypes.byref(b)))

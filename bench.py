@@ -627,6 +627,8 @@ def run_adaptive(args):
             big = amag >= 0.01 * scale_a
             ra = err[big] / amag[big]
             rec[tag] = {"sample": int(m), "dens_rel_max": float(rd.max()), "dens_rel_mean": float(rd.mean()),
+                        "dens_rel_p999": float(np.percentile(rd, 99.9)),
+                        "dens_frac_over_1e-5": float((rd > 1e-5).mean()),
                         "acc_rel_max": float(ra.max()), "acc_rel_p99": float(np.percentile(ra, 99)),
                         "acc_rel_median": float(np.median(ra)), "acc_err_max_over_rms": float(err.max() / scale_a),
                         "acc_err_max_over_g": float(err.max() / abs(float(sc.config.gravity))),
@@ -636,6 +638,8 @@ def run_adaptive(args):
     clk = clocks.stop()
     sol.sync()
     dens_max = max(c[t]["dens_rel_max"] for c in checks for t in ("low", "high") if t in c)
+    dens_p999 = max(c[t]["dens_rel_p999"] for c in checks for t in ("low", "high") if t in c)
+    dens_frac = max(c[t]["dens_frac_over_1e-5"] for c in checks for t in ("low", "high") if t in c)
     acc_rms = max(c[t]["acc_err_max_over_rms"] for c in checks for t in ("low", "high") if t in c)
     acc_g = max(c[t]["acc_err_max_over_g"] for c in checks for t in ("low", "high") if t in c)
     timed_steps = K - len(checks) if K > len(checks) else K
@@ -647,8 +651,9 @@ def run_adaptive(args):
                        "flags": int(sc.config.flags), "check_every": every,
                        "l2": "inputs larger than L2 (8M-particle state)"},
             "mass_exact_all_checks": all(c["mass_exact"] for c in checks),
-            "splits": splits, "removed": removed,
-            "fp64_sample": {"dens_rel_max": dens_max, "acc_err_max_over_rms": acc_rms, "acc_err_max_over_g": acc_g,
+            "splits_total": sol.counts()["total_split"], "removed_total": sol.counts()["total_removed"],
+            "fp64_sample": {"dens_rel_max": dens_max, "dens_rel_p999": dens_p999, "dens_frac_over_1e-5": dens_frac,
+                            "acc_err_max_over_rms": acc_rms, "acc_err_max_over_g": acc_g,
                             "checks": len(checks),
                             "tolerance": "dens 1e-5 relative"},
             "checks": checks, "clocks": clk, "gpu_launches": done * 14}

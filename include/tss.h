@@ -297,6 +297,8 @@ typedef struct tss_counts {
     long long steps;          /* steps taken                                          */
     unsigned error_bits;      /* device error word (TSS_ERR_*)                        */
     int n_removed_last;       /* high-res particles removed by merges in the last step */
+    long long total_split;    /* splits since creation                                 */
+    long long total_removed;  /* high-res particles removed by merges since creation   */
 } tss_counts;
 
 #define TSS_ERR_CAPACITY 0x1u /* a split would overflow the high-res pool            */

@@ -88,7 +88,8 @@ class TssConfig(ctypes.Structure):
 class TssCounts(ctypes.Structure):
     _fields_ = [("n_low", ctypes.c_int), ("n_high", ctypes.c_int), ("n_transient_low", ctypes.c_int),
                 ("n_split_last", ctypes.c_int), ("steps", ctypes.c_longlong), ("error_bits", ctypes.c_uint),
-                ("n_removed_last", ctypes.c_int)]
+                ("n_removed_last", ctypes.c_int), ("total_split", ctypes.c_longlong),
+                ("total_removed", ctypes.c_longlong)]
 
 
 class TssScaleState(ctypes.Structure):

@@ -538,6 +538,8 @@ tss_status tss_solver_counts(tss_solver* s, tss_counts* out) {
     out->steps = c.steps;
     out->error_bits = c.err;
     out->n_removed_last = c.dropped;
+    out->total_split = c.total_split;
+    out->total_removed = c.total_removed;
     return TSS_OK;
 }
 

@@ -727,6 +727,8 @@ __global__ void k_step_finish(Counters* c) {
         c->h_state0 = 0;
         c->steps += 1;
         c->dropped = c->n_drop;
+        c->total_split += c->n_split;
+        c->total_removed += c->n_drop;
         c->n_drop = 0;
     }
 }

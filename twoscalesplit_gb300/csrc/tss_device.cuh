@@ -58,6 +58,8 @@ struct Counters {
     int sorted[2];   // particles sorted in the last step (its `cur` counts)
     int n_drop;      // high-res list entries removed (state 2) in this step
     int dropped;     // ... in the last step: they are still in the list until the next build
+    long long total_split;    // splits since creation
+    long long total_removed;  // high-res particles removed by merges since creation
 };
 
 __device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating

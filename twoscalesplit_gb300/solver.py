@@ -65,7 +65,7 @@ class Solver:
         self._check(self.lib.tss_solver_counts(self.h, ctypes.byref(c)))
         return {"n_low": c.n_low, "n_high": c.n_high, "n_transient_low": c.n_transient_low,
                 "n_split_last": c.n_split_last, "steps": c.steps, "error_bits": c.error_bits,
-                "n_removed_last": c.n_removed_last}
+                "n_removed_last": c.n_removed_last, "total_split": c.total_split, "total_removed": c.total_removed}
 
     def download(self, scale):
         c = self.counts()

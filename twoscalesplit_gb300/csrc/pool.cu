@@ -645,6 +645,7 @@ tss_status tss_batch_create(int n_scenes, const tss_scene_desc* scenes, int cap_
     tss_solver* s = nullptr;
     tss_status st = create_pool(c, false, &s);
     if (st != TSS_OK) return st;
+    s->blocksL = (s->nL + 255) / 256;  // the low-res list is full: one block per 256 particles
     // ids are handed out lowest first, so scene k gets id k
     for (int k = 0; k < n_scenes; ++k) {
         int id = -1;

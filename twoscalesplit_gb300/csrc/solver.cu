@@ -421,7 +421,9 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
     s->H.g = grid_bufs_carve(gH, cap_high > 0 ? cap_high : 1, s->CH);
     GridBufs gw = grid_bufs_carve(gW, n_wall > 0 ? n_wall : 1, s->CL);
     s->woff = gw.off;
-    s->blocksL = particle_blocks(n_low > 0 ? n_low : 1, 256);
+    // one block per 256 low-res particles (their count is fixed): every block of the
+    // gathers does one tile of work, which balances better than a capped grid-stride launch
+    s->blocksL = n_low > 0 ? (n_low + 255) / 256 : 1;
     s->blocksH = particle_blocks(cap_high > 0 ? cap_high : 1, 256);
 
     if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {

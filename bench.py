@@ -434,25 +434,17 @@ def run_serve(args):
                                              pool_config_for_budget)
     from twoscalesplit_gb300.solver import Batch, Solver
     build.build()
+    world, rank, local = _dist()
+    if world > 1:
+        return run_serve_replicas(args, world, rank, local)
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     # 1. capacity of the batched step on the 512-scene mixed batch
     if args.capacity_lps:
         cap_lps, cap_src = args.capacity_lps, "given on the command line"
     else:
-        scs = scenes.mixed_batch(512, seed=0)
-        b = Batch(scs)
-        b.step(3)
-        torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        b.step(10)
-        e1.record()
-        torch.cuda.synchronize(dev)
-        b.sync()
-        cap_lps = sum(sc.n_low for sc in scs) * 10 / (e0.elapsed_time(e1) / 1e3)
+        cap_lps = measure_batch_capacity(dev)
         cap_src = "mixed_batch_512, 10 steps after 3 warm-up steps"
-        del b, scs
     # 2. the request stream
     rate = args.load * cap_lps / scenes.mean_work()
     trace = scenes.serving_trace(args.requests, rate, seed=args.seed)
@@ -544,6 +536,79 @@ def run_serve(args):
                     "d2h_bytes_per_step": float(sum(29 * 5 * sc.n_low for sc, _, _ in trace)) / max(summ["steps"], 1)},
             "gpu_launches": gpu_launches, "clocks": clk}
     print(json.dumps(line), flush=True)
+
+
+def measure_batch_capacity(dev, steps=10):
+    """Low-res particle-steps/s of the batched step on the 512-scene mixed batch."""
+    import torch
+    from twoscalesplit_gb300 import scenes
+    from twoscalesplit_gb300.solver import Batch
+    scs = scenes.mixed_batch(512, seed=0)
+    b = Batch(scs)
+    b.step(3)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.step(steps)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    b.sync()
+    return sum(sc.n_low for sc in scs) * steps / (e0.elapsed_time(e1) / 1e3)
+
+
+def run_serve_replicas(args, world, rank, local):
+    """The serving workload on `world` GPUs: independent replicas behind a
+    deterministic least-work dispatcher, no exchange in the data path (weak
+    scaling: the stream has `world` times the requests and arrival rate of the
+    one-GPU stream).  Per-request statistics are merged over gloo; rank 0 prints."""
+    import torch
+    import torch.distributed as dist
+    from twoscalesplit_gb300 import _abi, dispatch, scenes
+    from twoscalesplit_gb300.serving import Request, Server, latency_summary, pool_config_for_budget
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist.init_process_group("gloo")
+    cap = args.capacity_lps or measure_batch_capacity(dev)
+    cap = dispatch.gather(cap)[0]  # every replica uses rank 0's measurement
+    rate = world * args.load * cap / scenes.mean_work()
+    trace = scenes.serving_trace(args.requests * world, rate, seed=args.seed)
+    n_low = np.array([sc.n_low for sc, _, _ in trace], dtype=np.float64)
+    cells = np.array([sc.config.dims_low[0] * sc.config.dims_low[1] for sc, _, _ in trace], dtype=np.float64)
+    walls = np.array([sc.n_wall for sc, _, _ in trace], dtype=np.float64)
+    cfg = pool_config_for_budget(int(args.budget_gb * (1 << 30)), 1.25 * cells.sum() / n_low.sum() + 0.05,
+                                 1.25 * walls.sum() / n_low.sum() + 0.05, max_scenes=8192)
+    sv = Server(cfg, max_steps_per_launch=args.chunk, max_in_flight=2, staging_bytes=2 << 30)
+    warm = scenes.serving_trace(4, 1e3, seed=args.seed + 1, n_min=2000, n_max=20000, h_min=10, h_max=20)
+    sv.run([Request(sc, h, t) for sc, h, t in warm])
+    reqs = [Request(sc, h, t) for sc, h, t in trace]
+    dist.barrier()
+    clocks = ClockSampler(str(local))
+    clocks.start()
+    stats, summ = dispatch.serve_replicated(reqs, lambda rs: sv.run(rs)[:2], rank, world)
+    clk = clocks.stop()
+    if rank == 0:
+        served = [k for k, st in enumerate(stats) if st["status"] in (_abi.TSS_OK, _abi.TSS_NUMERIC)]
+        horizons = np.array([h for _, h, _ in trace], dtype=np.float64)
+        arrivals = np.array([t for _, _, t in trace])
+        makespan = summ["makespan_s"] - float(arrivals.min())
+        ss = float(horizons[served].sum())
+        line = {"metric": "scene-steps/s", "value": ss / makespan, "unit": "scene-steps/s", "n_gpus": world,
+                "steps": int(summ["steps"]), "warmup": 1, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"serving_{len(trace)}_poisson", "requests": len(trace),
+                           "arrival_rate_per_s": rate, "load": args.load, "replicas": world,
+                           "dispatch": "least assigned work (n_low x horizon), arrival order",
+                           "capacity_low_particle_steps_per_s": cap, "hbm_budget_gb_per_gpu": args.budget_gb,
+                           "parallelism": f"replicas{world}"},
+                "served": len(served), "latency_s": latency_summary(stats),
+                "low_particle_steps_per_s": float(n_low[served] @ horizons[served]) / makespan,
+                "e2e": {"value": ss / makespan, "unit": "scene-steps/s",
+                        "h2d_bytes_per_step": float(sum(16 * sc.n_low + 8 * sc.n_wall for sc, _, _ in trace))
+                        / max(summ["steps"], 1),
+                        "d2h_bytes_per_step": float(sum(29 * 5 * sc.n_low for sc, _, _ in trace)) / max(summ["steps"], 1)},
+                "gpu_launches": int(summ["steps"] * 14 + len(served) * 16), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    dist.destroy_process_group()
 
 
 def run_adaptive(args):

@@ -144,3 +144,29 @@ def test_server_results_equal_alone_and_admission_waits_for_memory():
     # memory-bound admission: some request waited for an earlier one to finish
     done_first = min(stats[k]["done_s"] for k in served)
     assert any(stats[k]["admit_s"] >= done_first - 1e-3 for k in served)
+
+
+def test_pool_moving_roi_and_merge_start_at_each_scenes_own_step():
+    # scenes with a translating region of interest and merging, admitted at different
+    # pool steps: each one's region starts moving at its own first step, so each
+    # equals the same scene run alone
+    A = scenes.adaptive_dam_break(30, 60, 0.4 / 30, roi_velocity=(14.0, 3.0), roi_start=(0.0, 0.05), steps=60)
+    B = scenes.adaptive_dam_break(24, 40, 0.4 / 24, roi_velocity=(-9.0, 2.0), roi_start=(0.25, 0.1), steps=60,
+                                  seed=4)
+    fa, fb = footprint(A), footprint(B)
+    cfg = pool_config(low_slots=fa["low_slots"] + fb["low_slots"], low_cells=fa["low_cells"] + fb["low_cells"],
+                      high_cells=fa["high_cells"] + fb["high_cells"],
+                      wall_particles=fa["wall_particles"] + fb["wall_particles"], max_scenes=4)
+    pool = Pool(cfg)
+    a = pool.admit(A)
+    pool.step(17)
+    b = pool.admit(B)
+    pool.step(40)
+    got_a, got_b = pool.extract(a), pool.extract(b)
+    pool.sync()
+    for got in (got_a, got_b):
+        got[1] = {k: v[got[1]["state"] != 2] for k, v in got[1].items()}  # removed in the last step
+    _assert_same(_alone(A, 57), got_a, "A")
+    _assert_same(_alone(B, 40), got_b, "B")
+    c = pool.counts()
+    assert c["total_split"] > 0 and c["total_removed"] > 0

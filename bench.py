@@ -565,6 +565,8 @@ def run_serve_replicas(args, world, rank, local):
     import torch.distributed as dist
     from twoscalesplit_gb300 import _abi, dispatch, scenes
     from twoscalesplit_gb300.serving import Request, Server, latency_summary, pool_config_for_budget
+    # replicas never wait on one another, so ranks beyond the visible devices share them
+    local = local % torch.cuda.device_count()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     dist.init_process_group("gloo")

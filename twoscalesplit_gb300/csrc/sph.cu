@@ -19,7 +19,7 @@ namespace tss {
 namespace {
 __device__ __forceinline__ int nthreads() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ int tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return sub2(a, b); }
 }  // namespace
 
 

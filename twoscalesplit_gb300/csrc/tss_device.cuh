@@ -64,6 +64,36 @@ struct Counters {
 
 __device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating
 
+// Packed FP32 pairs: the sm_100+ add/sub/mul .f32x2 instructions do two IEEE
+// round-to-nearest operations in one issue slot, each component rounded exactly as
+// the scalar operation (checked bit for bit against the scalar forms, subnormals
+// included), so packing the x and y halves of an expression changes no result.
+__device__ __forceinline__ unsigned long long pk(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 upk(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+    return upk(d);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+    return upk(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+    return upk(d);
+}
+
 // computeGridCoordinate(pos, offset), WCSPHSolver.cu:265-289
 __device__ __forceinline__ void grid_coord(float px, float py, float off, float ox, float oy, float cell,
                                            int dimx, int dimy, int& cx, int& cy) {
@@ -99,7 +129,7 @@ __device__ __forceinline__ float2 kernDW(float2 x, float d, float rad, float G) 
     const float n1 = G * (a * a - 4.0f * b * b);
     const float n2 = G * a * a;
     const float c = (q < 1.0f ? n1 : n2) / d;
-    return q < 2.0f ? make_float2(c * x.x, c * x.y) : make_float2(0.0f, 0.0f);
+    return q < 2.0f ? mul2(make_float2(c, c), x) : make_float2(0.0f, 0.0f);
 }
 
 // evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114 (selected, as above)
@@ -133,18 +163,19 @@ __device__ __forceinline__ bool notDeleted(unsigned s) { return s < 2u; }       
 // qi, qj are p/rho^2 of the two particles (the reference's pre/dens2, prej/densj2).
 __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float dist, float2 vij, float qi, float qj,
                                            float densi, float densj, float h, float2& acc, float2& accT) {
-    const float dvp = vij.x * pij.x + vij.y * pij.y;
+    const float2 vp = mul2(vij, pij);
+    const float dvp = vp.x + vp.y;
     const float visc = dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
     float coeff = qi + qj;
     coeff = dvp < 0.0f ? coeff - visc : coeff;  // the reference's `if (dvp < 0) coeff -= ...`
     float2 gI = kernDW(pij, dist, P.r, P.GL);
     float2 gJ = kernDW(pij, dist, P.rh, P.GH);
-    acc.x += coeff * (gI.x + gJ.x) / 2.0f;
-    acc.y += coeff * (gI.y + gJ.y) / 2.0f;
+    const float2 half = make_float2(0.5f, 0.5f);  // x / 2 == x * 0.5 exactly
+    acc = add2(acc, mul2(mul2(make_float2(coeff, coeff), add2(gI, gJ)), half));
     float w = kernW(dist, P.r, P.CL);
     float w2 = kernW(dist, P.rh, P.CH);
-    accT.x += pij.x * (w + w2) / 2.0f;
-    accT.y += pij.y * (w + w2) / 2.0f;
+    const float ww = w + w2;
+    accT = add2(accT, mul2(mul2(pij, make_float2(ww, ww)), half));
 }
 
 // Candidates of a cell window, row by row (cells in x order, particles in cell
@@ -184,7 +215,10 @@ struct Window {
     }
 };
 
-__device__ __forceinline__ float sq(float2 v) { return v.x * v.x + v.y * v.y; }
+__device__ __forceinline__ float sq(float2 v) {
+    const float2 m = mul2(v, v);
+    return m.x + m.y;
+}
 
 
 

@@ -64,35 +64,13 @@ struct Counters {
 
 __device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating
 
-// Packed FP32 pairs: the sm_100+ add/sub/mul .f32x2 instructions do two IEEE
-// round-to-nearest operations in one issue slot, each component rounded exactly as
-// the scalar operation (checked bit for bit against the scalar forms, subnormals
-// included), so packing the x and y halves of an expression changes no result.
-__device__ __forceinline__ unsigned long long pk(float2 a) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 upk(unsigned long long r) {
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
+// Packed FP32 pairs: sm_100's two-wide add and multiply (__fadd2_rn, __fmul2_rn)
+// round each component exactly as __fadd_rn / __fmul_rn do, which are never merged
+// into a multiply-add, so packing the x and y halves of an expression changes no
+// result.  a - b is a + (-b) (IEEE defines subtraction so).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 
 // computeGridCoordinate(pos, offset), WCSPHSolver.cu:265-289
 __device__ __forceinline__ void grid_coord(float px, float py, float off, float ox, float oy, float cell,

@@ -471,7 +471,7 @@ def run_serve(args):
     service = np.zeros(len(trace))
     exact = 0
     plain_steps_ms = 0.0
-    for k, (sc, h, _) in enumerate(trace):
+    for k, (sc, h, _) in enumerate(trace if not args.no_plain else []):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         sol = Solver.from_scene(sc)
@@ -489,16 +489,29 @@ def run_serve(args):
             exact += int(same)
         del sol
     arrivals = np.array([t for _, _, t in trace])
-    plain_done = fifo_schedule(arrivals, service)
-    plain_lat = plain_done - arrivals
     horizons = np.array([h for _, h, _ in trace], dtype=np.float64)
     scene_steps = float(horizons[served].sum())
     makespan = summ["makespan_s"] - float(arrivals.min())
-    plain_makespan = float(plain_done.max() - arrivals.min())
-    # 4. saturated: the first `burst` requests at once
-    nb = min(args.burst, len(trace))
-    st_b, summ_b, _ = sv.run([Request(sc, h, 0.0) for sc, h, _ in trace[:nb]])
-    burst_ss = float(sum(h for _, h, _ in trace[:nb]))
+    plain_part, saturated = None, None
+    if not args.no_plain:
+        plain_done = fifo_schedule(arrivals, service)
+        plain_lat = plain_done - arrivals
+        plain_makespan = float(plain_done.max() - arrivals.min())
+        plain_part = {
+            "scene_steps_per_s": float(horizons.sum()) / plain_makespan,
+            "latency_s": {"p50_s": float(np.percentile(plain_lat, 50)), "p99_s": float(np.percentile(plain_lat, 99)),
+                          "mean_s": float(plain_lat.mean())},
+            "service_s_total": float(service.sum()),
+            "how": "each request timed through the plain solver (create, horizon steps, download); FIFO "
+                   "completion times from those service times and the same arrivals"}
+        # 4. saturated: the first `burst` requests at once
+        nb = min(args.burst, len(trace))
+        st_b, summ_b, _ = sv.run([Request(sc, h, 0.0) for sc, h, _ in trace[:nb]])
+        burst_ss = float(sum(h for _, h, _ in trace[:nb]))
+        saturated = {"requests": nb, "scene_steps_per_s": burst_ss / summ_b["makespan_s"],
+                     "plain_scene_steps_per_s": burst_ss / float(service[:nb].sum()),
+                     "speedup_vs_plain": float(service[:nb].sum()) / summ_b["makespan_s"],
+                     "mean_active_scenes": summ_b["mean_active"]}
     gpu_launches = int(summ["steps"] * 14 + len(served) * 16)
     line = {"metric": "scene-steps/s", "value": scene_steps / makespan, "unit": "scene-steps/s", "n_gpus": 1,
             "steps": int(summ["steps"]), "warmup": 1, "higher_is_better": True, "scaling": "weak",
@@ -516,21 +529,12 @@ def run_serve(args):
             "served": len(served), "rejected": int(sum(1 for st in stats if st["status"] == _abi.TSS_INVALID_ARG)),
             "latency_s": lat, "low_particle_steps_per_s": float(n_low[served] @ horizons[served]) / makespan,
             "mean_active_scenes": summ["mean_active"], "max_active_scenes": summ["max_active"],
-            "plain_one_at_a_time": {
-                "scene_steps_per_s": float(horizons.sum()) / plain_makespan,
-                "latency_s": {"p50_s": float(np.percentile(plain_lat, 50)), "p99_s": float(np.percentile(plain_lat, 99)),
-                              "mean_s": float(plain_lat.mean())},
-                "service_s_total": float(service.sum()),
-                "how": "each request timed through the plain solver (create, horizon steps, download); FIFO "
-                       "completion times from those service times and the same arrivals"},
-            "speedup_vs_plain": (scene_steps / makespan) / (float(horizons.sum()) / plain_makespan),
-            "saturated": {"requests": nb, "scene_steps_per_s": burst_ss / summ_b["makespan_s"],
-                          "plain_scene_steps_per_s": burst_ss / float(service[:nb].sum()),
-                          "speedup_vs_plain": float(service[:nb].sum()) / summ_b["makespan_s"],
-                          "mean_active_scenes": summ_b["mean_active"]},
-            "exact_vs_alone": f"{exact}/{len(verify)} requests bit-identical to the plain solver",
-            "non_finite": {"served": numeric_served, "plain": numeric_plain,
-                           "same_requests": numeric_served == numeric_plain},
+            "plain_one_at_a_time": plain_part,
+            "speedup_vs_plain": None if plain_part is None else (scene_steps / makespan) / plain_part["scene_steps_per_s"],
+            "saturated": saturated,
+            "exact_vs_alone": None if args.no_plain else f"{exact}/{len(verify)} requests bit-identical to the plain solver",
+            "non_finite": {"served": numeric_served, "plain": None if args.no_plain else numeric_plain,
+                           "same_requests": None if args.no_plain else numeric_served == numeric_plain},
             "e2e": {"value": scene_steps / makespan, "unit": "scene-steps/s",
                     "h2d_bytes_per_step": float(sum(16 * sc.n_low + 8 * sc.n_wall for sc, _, _ in trace)) / max(summ["steps"], 1),
                     "d2h_bytes_per_step": float(sum(29 * 5 * sc.n_low for sc, _, _ in trace)) / max(summ["steps"], 1)},
@@ -747,6 +751,7 @@ def main():
     ap.add_argument("--burst", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--capacity-lps", type=float, default=0.0)
+    ap.add_argument("--no-plain", action="store_true", help="serve workload: skip the plain-solver comparison")
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)

@@ -277,6 +277,8 @@ tss_status tss_server_create(const tss_server_config* cfg, tss_server** out);
 tss_status tss_server_run(tss_server* sv, int n, const tss_request* reqs, tss_request_stats* stats,
                           tss_serve_summary* summary);
 void tss_server_destroy(tss_server* sv);
+/* Text of the last failure of a server call (or of its pool's last call). */
+tss_status tss_server_last_error(tss_server* sv, char* buf, int len);
 
 /* Advance n_steps steps (WCSPHSolver::AdvanceTS, WCSPHSolver.cu:2726-2810), enqueued
  * on `stream` (a cudaStream_t; NULL = the default stream, as the reference used).

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <new>
@@ -193,15 +194,19 @@ struct Run {
     int max_active = 0;
     int served = 0;
     double last_done = 0;
-    tss_status status = TSS_OK;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
     // Wait for the oldest chunk: completion times, result copies, ring space.
+    tss_status fail(tss_status st, const char* msg) {
+        sv->err = msg;
+        return st;
+    }
+
     tss_status complete_oldest() {
         Chunk c = std::move(inflight.front());
         inflight.pop_front();
-        if (cudaEventSynchronize(c.ev) != cudaSuccess) return TSS_CUDA_ERROR;
+        if (cudaEventSynchronize(c.ev) != cudaSuccess) return fail(TSS_CUDA_ERROR, "waiting for a chunk of steps");
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, sv->ev0, c.ev);
         const double t = ms / 1e3;
@@ -236,7 +241,8 @@ struct Run {
 
     tss_status record_open() {
         open.ev = sv->event();
-        if (!open.ev || cudaEventRecord(open.ev, sv->stream) != cudaSuccess) return TSS_CUDA_ERROR;
+        if (!open.ev || cudaEventRecord(open.ev, sv->stream) != cudaSuccess)
+            return fail(TSS_CUDA_ERROR, "recording a chunk's event");
         inflight.push_back(std::move(open));
         open = Chunk{};
         return TSS_OK;
@@ -275,7 +281,7 @@ struct Run {
         }
         int id = -1;
         tss_status st = tss_pool_admit(sv->pool, &s, sv->stream, &id);
-        if (st != TSS_OK) return st == TSS_CAPACITY ? TSS_CUDA_ERROR : st;  // can_admit said it fits
+        if (st != TSS_OK) return fail(st == TSS_CAPACITY ? TSS_CUDA_ERROR : st, "admission failed after the pool reported room");
         active.push_back({r, id, reqs[r].horizon, steps});
         stats[r].admit_s = now();
         stats[r].first_step = steps;
@@ -296,7 +302,7 @@ struct Run {
             if (!open.done.empty() || open.n_in || open.n_out) {
                 if (tss_status st = record_open(); st != TSS_OK) return st;
             }
-            if (inflight.empty()) return TSS_CUDA_ERROR;  // nothing left to free
+            if (inflight.empty()) return fail(TSS_CAPACITY, "no room for a result in the empty result ring");
             if (tss_status st = complete_oldest(); st != TSS_OK) return st;
         }
         ++open.n_out;
@@ -348,9 +354,21 @@ tss_status tss_server_create(const tss_server_config* cfg, tss_server** out) {
 
 void tss_server_destroy(tss_server* sv) { delete sv; }
 
+tss_status tss_server_last_error(tss_server* sv, char* buf, int len) {
+    if (!sv || !buf || len <= 0) return TSS_INVALID_ARG;
+    std::string msg = sv->err;
+    if (msg.empty() && sv->pool) {  // a pool call's own message
+        char pbuf[512];
+        if (tss_solver_last_error(sv->pool, pbuf, sizeof pbuf) == TSS_OK) msg = pbuf;
+    }
+    std::snprintf(buf, static_cast<size_t>(len), "%s", msg.c_str());
+    return TSS_OK;
+}
+
 tss_status tss_server_run(tss_server* sv, int n, const tss_request* reqs, tss_request_stats* stats,
                           tss_serve_summary* summary) {
     if (!sv || n < 0 || (n > 0 && (!reqs || !stats))) return TSS_INVALID_ARG;
+    sv->err.clear();
     for (int i = 0; i < n; ++i)
         if (reqs[i].horizon < 1 || !(reqs[i].arrival_s >= 0.0)) return TSS_INVALID_ARG;
     std::vector<int> order(static_cast<size_t>(n));

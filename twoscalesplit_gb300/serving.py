@@ -208,7 +208,9 @@ class Server:
         summ = _abi.TssServeSummary()
         st = self.lib.tss_server_run(self.h, n, reqs, stats, ctypes.byref(summ))
         if st != _abi.TSS_OK:
-            raise TssError(st, "tss_server_run")
+            buf = ctypes.create_string_buffer(512)
+            self.lib.tss_server_last_error(self.h, buf, 512)
+            raise TssError(st, "tss_server_run: " + buf.value.decode(errors="replace"))
         out_stats = []
         for k in range(n):
             s = stats[k]

@@ -162,6 +162,20 @@ def cpu_baseline(scene_name, seed, budget_s, threads=None):
                       f"{dt:.1f} s), FP32 CPU restatement of the reference step, OpenMP"}
 
 
+def tuned_shape(sol, kind, n_low, args):
+    """The gathers' launch shape for this GPU and workload class: from the launch
+    cache, else tuned on `sol` (its trial steps advance its state: call during
+    warm-up).  --no-autotune keeps the default shape."""
+    if args.no_autotune:
+        return sol.launch, 0
+    from twoscalesplit_gb300 import tuning
+    return tuning.tuned_launch(sol, kind, n_low, path=args.launch_cache)
+
+
+def compact_shape(shape):
+    return {g: f"{v['threads']}{'p' if v['persistent'] else ''}" for g, v in shape.items()}
+
+
 def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
@@ -226,9 +240,11 @@ def run_ours(args):
         sol.set_fresh(np.zeros(0, np.int32))
 
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
-    # warm-up (graph capture happens here)
+    # warm-up (graph capture happens here), then the launch-shape autotuner on the
+    # same state (its trial steps are warm-up too: the state is reset after them)
     sol.step(max(args.warmup, 1), stream=sh)
     torch.cuda.synchronize(dev)
+    shape, tune_steps = tuned_shape(sol, "single", sc.n_low, args)
     reset()
     K = args.steps
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
@@ -330,7 +346,8 @@ def run_ours(args):
         "config": {"workload": args.scene, "n_low": sc.n_low, "n_high_end": c_end["n_high"],
                    "cap_high": sc.cap_high, "dt": cfg.dt, "relax_iters": cfg.relax_iters,
                    "q1_compat": bool(cfg.flags & 1), "l2": "flushed between timed steps (512 MiB write)",
-                   "parallelism": f"replicas{world}", "seed": 0},
+                   "parallelism": f"replicas{world}", "seed": 0, "launch": compact_shape(shape),
+                   "autotune_steps": tune_steps},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
                      "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": measured_traffic(top),
                      "traffic_source": "profiles/dram_traffic.txt (ncu, one launch)",
@@ -371,6 +388,7 @@ def run_batch(args):
              "state": np.zeros(0, np.uint8)}
     b.step(max(args.warmup, 1), stream=sh)
     torch.cuda.synchronize(dev)
+    shape, tune_steps = tuned_shape(b, "batch", sum(sc.n_low for sc in scs), args)
     b.upload(0, init)
     b.upload(1, empty)
     b.set_fresh(np.zeros(0, np.int32))
@@ -396,6 +414,7 @@ def run_batch(args):
     for sc in scs[:n_plain]:
         sol = Solver.from_scene(sc)
         sol.step(max(args.warmup, 1), stream=sh)
+        tuned_shape(sol, "single", sc.n_low, args)
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -410,6 +429,7 @@ def run_batch(args):
             "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": batch_ms / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"mixed_batch_{len(scs)}", "scenes": len(scs), "n_low_total": n_low,
+                       "launch": compact_shape(shape), "autotune_steps": tune_steps,
                        "n_high_end": c["n_high"], "l2": "flushed between timed steps (512 MiB write)"},
             "particle_steps_per_s": n_low * K / (batch_ms / 1e3),
             "plain_one_at_a_time": {"scene_steps_per_s": len(scs) * K / (plain_ms / 1e3),
@@ -752,6 +772,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--capacity-lps", type=float, default=0.0)
     ap.add_argument("--no-plain", action="store_true", help="serve workload: skip the plain-solver comparison")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape of the gathers")
+    ap.add_argument("--launch-cache", default=None, help="launch-shape cache file (default: the user cache)")
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)

@@ -283,8 +283,10 @@ tss_status tss_server_last_error(tss_server* sv, char* buf, int len);
 /* Advance n_steps steps (WCSPHSolver::AdvanceTS, WCSPHSolver.cu:2726-2810), enqueued
  * on `stream` (a cudaStream_t; NULL = the default stream, as the reference used).
  * Nothing is copied back to the host; the particle counts stay on the device.  The
- * first call captures the step into a CUDA graph (on a private stream); later calls
- * replay it. */
+ * steps are replayed from CUDA graphs of 8, 4, 2 and 1 steps (n_steps taken as a
+ * sum of those buckets; each graph is captured on a private stream at its first
+ * use and does not depend on the particle counts).  With profiling on, every step
+ * is its own graph. */
 tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream);
 
 /* Block until all enqueued work is done; returns the device error word mapped to a
@@ -374,6 +376,28 @@ tss_status tss_solver_device_buffers(tss_solver* s, tss_buffers* out);
 #define TSS_NUM_STAGES 8
 tss_status tss_solver_profile(tss_solver* s, int enable);
 tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n);
+
+/* Launch shape of the four gather kernels, indexed high-res density, low-res
+ * density, low-res force, high-res force (stages 3, 4, 5, 7).  Every kernel walks
+ * its list with a grid-stride loop over a device-side count, so results do not
+ * depend on the shape.  The reference launched 256-thread blocks covering the
+ * list (WCSPHSolver.cu:2421,2437); that shape is the default here. */
+#define TSS_NUM_GATHERS 4
+typedef struct tss_launch {
+    int threads[TSS_NUM_GATHERS];     /* threads per block: 64, 128 or 256 (one particle per thread) */
+    int persistent[TSS_NUM_GATHERS];  /* 0: blocks cover the list's capacity (at most 4096 threads
+                                         per SM, grid-striding beyond); 1: one wave of resident
+                                         blocks (SMs x blocks per SM), each striding over the list */
+} tss_launch;
+tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out);
+/* Replaces the launch shape (the step graphs are captured again at the next step). */
+tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in);
+/* Launch-shape autotuner: times every candidate shape (threads 64/128/256, covering
+ * or persistent grids) on this handle's own steps, keeps the fastest shape of each
+ * gather and installs it.  The trial steps are real steps of the handle's state
+ * (the shape does not change results); *steps_taken (may be NULL) receives how many
+ * were taken: 6 x (steps_per_trial + 1).  Synchronises. */
+tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* best, int* steps_taken);
 
 /* Last error message of this handle (NUL-terminated, truncated to len). */
 tss_status tss_solver_last_error(tss_solver* s, char* buf, int len);

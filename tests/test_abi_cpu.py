@@ -79,3 +79,24 @@ def test_status_strings_and_argument_checks(lib):
     assert lib.tss_solver_create(ctypes.byref(c), -1, None, None, 1.0, 0, 1.0, 0, None, 1.0,
                                  ctypes.byref(out)) == _abi.TSS_INVALID_ARG
     assert lib.tss_solver_step(None, 1, None) == _abi.TSS_INVALID_ARG
+
+
+def test_launch_struct_layout_and_argument_checks(lib, tmp_path):
+    # the ctypes mirror of tss_launch has the C layout
+    src = tmp_path / "sz.c"
+    src.write_text('#include "tss.h"\n#include <stdio.h>\n#include <stddef.h>\n'
+                   'int main(void){printf("%zu %zu\\n", sizeof(tss_launch), offsetof(tss_launch, persistent));'
+                   'return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include", str(src),
+                           "-o", str(exe)])
+    size, off = map(int, subprocess.check_output([str(exe)]).split())
+    assert size == ctypes.sizeof(_abi.TssLaunch) and off == _abi.TssLaunch.persistent.offset
+    shape = {g: {"threads": t, "persistent": p} for g, t, p in zip(_abi.GATHER_NAMES, (64, 128, 256, 64),
+                                                                      (True, False, False, True))}
+    assert _abi.TssLaunch.from_dict(shape).as_dict() == shape
+    l = _abi.TssLaunch()
+    assert lib.tss_solver_get_launch(None, ctypes.byref(l)) == _abi.TSS_INVALID_ARG
+    assert lib.tss_solver_set_launch(None, ctypes.byref(l)) == _abi.TSS_INVALID_ARG
+    n = ctypes.c_int(0)
+    assert lib.tss_solver_autotune(None, 1, ctypes.byref(l), ctypes.byref(n)) == _abi.TSS_INVALID_ARG

@@ -1,0 +1,108 @@
+"""Launch shapes, the autotuner and the step-bucket graphs: none of them may change a
+result.  Every gather walks its list with a grid-stride loop over a device-side
+count, so any block size and grid gives the same sums in the same order; the step
+graphs of 2, 4 and 8 steps replay the same kernels as the one-step graph."""
+import itertools
+import math
+
+import numpy as np
+import pytest
+
+from twoscalesplit_gb300 import scenes
+from twoscalesplit_gb300._abi import GATHER_NAMES, TSS_SCALE_HIGH, TSS_SCALE_LOW, TssError
+from twoscalesplit_gb300.solver import Batch, Solver
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from twoscalesplit_gb300 import build
+    build.build()
+
+
+def _scene(seed=3, relax=4):
+    sc = scenes.dam_break_small(24, 40, seed=seed, relax_iters=relax)
+    sc.config.roi[:] = [0.2, -math.inf, math.inf, math.inf]
+    return sc
+
+
+def _state(sol):
+    return [sol.download(s) for s in (TSS_SCALE_LOW, TSS_SCALE_HIGH)]
+
+
+def _assert_same(a, b):
+    for sa, sb in zip(a, b):
+        for name in ("id", "pos", "vel", "state"):
+            assert np.array_equal(sa[name], sb[name]), name
+
+
+def _shape(threads, persistent):
+    return {g: {"threads": threads, "persistent": persistent} for g in GATHER_NAMES}
+
+
+def test_default_shape_is_the_reference_block_size():
+    sol = Solver.from_scene(_scene())
+    assert sol.launch == _shape(256, False)
+
+
+@pytest.mark.parametrize("threads,persistent", list(itertools.product([64, 128, 256], [False, True])))
+def test_every_shape_gives_the_same_steps(threads, persistent):
+    sc = _scene()
+    ref = Solver.from_scene(sc)
+    ref.step(60)
+    sol = Solver.from_scene(sc)
+    sol.set_launch(_shape(threads, persistent))
+    sol.step(60)
+    sol.sync()
+    assert sol.counts()["n_high"] > 0
+    _assert_same(_state(ref), _state(sol))
+
+
+def test_shape_of_a_batch_does_not_change_its_scenes():
+    scs = [_scene(seed=s, relax=0) for s in (5, 6, 7)]
+    a, b = Batch(scs), Batch(scs)
+    mixed = {g: {"threads": t, "persistent": p} for g, t, p in zip(GATHER_NAMES, (64, 128, 256, 64),
+                                                                      (True, False, True, False))}
+    b.set_launch(mixed)
+    a.step(50)
+    b.step(50)
+    for k in range(len(scs)):
+        for scale in (TSS_SCALE_LOW, TSS_SCALE_HIGH):
+            x, y = a.download_scene(k, scale), b.download_scene(k, scale)
+            for name in ("id", "pos", "vel", "state"):
+                assert np.array_equal(x[name], y[name]), (k, scale, name)
+
+
+def test_autotune_installs_a_valid_shape_and_keeps_the_trajectory():
+    sc = _scene(seed=11)
+    tuned = Solver.from_scene(sc)
+    shape, taken = tuned.autotune(steps_per_trial=2)
+    assert taken == 6 * 3
+    assert tuned.launch == shape
+    for g in GATHER_NAMES:
+        assert shape[g]["threads"] in (64, 128, 256)
+    tuned.step(7)
+    ref = Solver.from_scene(sc)
+    ref.step(taken + 7)
+    assert tuned.counts()["steps"] == ref.counts()["steps"] == taken + 7
+    _assert_same(_state(ref), _state(tuned))
+
+
+def test_invalid_shape_is_rejected_and_the_old_one_kept():
+    sol = Solver.from_scene(_scene())
+    with pytest.raises(TssError):
+        sol.set_launch(_shape(96, False))
+    assert sol.launch == _shape(256, False)
+
+
+def test_step_buckets_equal_single_steps():
+    sc = _scene(seed=9)
+    one = Solver.from_scene(sc)
+    for _ in range(29):
+        one.step(1)
+    many = Solver.from_scene(sc)
+    many.step(13)   # 8 + 4 + 1
+    many.step(16)   # 8 + 8
+    assert many.counts()["steps"] == 29
+    _assert_same(_state(one), _state(many))

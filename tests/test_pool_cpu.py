@@ -82,3 +82,31 @@ def test_serving_trace_distributions():
     n = np.array([sc.n_low for sc, _, _ in tr])
     assert n.min() >= 500 and n.max() <= 30000
     assert scenes.mean_work(1000, 500000, 200, 5000) == pytest.approx((499000 / math.log(500)) * 2600)
+
+
+def test_launch_cache_roundtrip(tmp_path):
+    from twoscalesplit_gb300 import tuning
+
+    class FakeSolver:
+        def __init__(self):
+            self.set = None
+            self.tuned = 0
+
+        def autotune(self, steps_per_trial):
+            self.tuned += 1
+            return {"force_low": {"threads": 128, "persistent": False}}, 6 * (steps_per_trial + 1)
+
+        def set_launch(self, shape):
+            self.set = shape
+
+    path = str(tmp_path / "launch.json")
+    assert tuning.workload_class("single", 999698) == "single/2^20"
+    s = FakeSolver()
+    shape, taken = tuning.tuned_launch(s, "single", 1000, path=path, steps_per_trial=2)
+    assert taken == 18 and s.tuned == 1 and s.set is None
+    s2 = FakeSolver()
+    shape2, taken2 = tuning.tuned_launch(s2, "single", 1100, path=path)
+    assert taken2 == 0 and s2.tuned == 0 and s2.set == shape == shape2
+    s3 = FakeSolver()
+    tuning.tuned_launch(s3, "batch", 1000, path=path)
+    assert s3.tuned == 1 and len(tuning.load(path)) == 2

@@ -42,6 +42,9 @@ TSS_NUM_STAGES = 8
 STAGE_NAMES = ["grid_high", "grid_low", "relax", "density_high", "density_low", "force_low", "split",
                "force_high"]
 
+TSS_NUM_GATHERS = 4
+GATHER_NAMES = ["density_high", "density_low", "force_low", "force_high"]
+
 TSS_ERR_CAPACITY = 0x1
 TSS_GRID_NOALLOC_MAX_BYTES = 32 << 20
 TSS_ERR_NUMERIC = 0x2
@@ -165,6 +168,23 @@ class TssView(ctypes.Structure):
                 ("width", ctypes.c_int), ("height", ctypes.c_int)]
 
 
+class TssLaunch(ctypes.Structure):
+    """struct tss_launch: threads per block and grid kind of each gather kernel."""
+    _fields_ = [("threads", ctypes.c_int * TSS_NUM_GATHERS), ("persistent", ctypes.c_int * TSS_NUM_GATHERS)]
+
+    def as_dict(self):
+        return {g: {"threads": self.threads[k], "persistent": bool(self.persistent[k])}
+                for k, g in enumerate(GATHER_NAMES)}
+
+    @classmethod
+    def from_dict(cls, d):
+        l = cls()
+        for k, g in enumerate(GATHER_NAMES):
+            l.threads[k] = int(d[g]["threads"])
+            l.persistent[k] = 1 if d[g]["persistent"] else 0
+        return l
+
+
 class TssBuffers(ctypes.Structure):
     _fields_ = [("pos", ctypes.c_void_p * 2), ("vel", ctypes.c_void_p * 2), ("dens", ctypes.c_void_p * 2),
                 ("id", ctypes.c_void_p * 2), ("state", ctypes.c_void_p * 2), ("counts", ctypes.c_void_p)]
@@ -236,6 +256,9 @@ def load_library(path=None):
         "tss_solver_last_error": (i, [vp, ctypes.c_char_p, i]),
         "tss_solver_profile": (i, [vp, i]),
         "tss_solver_stage_times": (i, [vp, fp, i]),
+        "tss_solver_get_launch": (i, [vp, ctypes.POINTER(TssLaunch)]),
+        "tss_solver_set_launch": (i, [vp, ctypes.POINTER(TssLaunch)]),
+        "tss_solver_autotune": (i, [vp, i, ctypes.POINTER(TssLaunch), ctypes.POINTER(i)]),
         "tss_status_string": (ctypes.c_char_p, [i]),
         "tss_grid_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
         "tss_batch_create": (i, [i, ctypes.POINTER(TssSceneDesc), i, ctypes.POINTER(vp)]),

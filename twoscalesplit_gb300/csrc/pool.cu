@@ -277,6 +277,11 @@ tss_status create_pool(const tss_pool_config& c, bool reserve_high, tss_solver**
     s->woff = s->gW.off;
     s->blocksL = particle_blocks(s->nL, 256);
     s->blocksH = particle_blocks(s->capH > 0 ? s->capH : 1, 256);
+    s->low_full = false;
+    if (tss_status la = s->apply_launch(default_launch()); la != TSS_OK) {
+        delete s;
+        return la;
+    }
     s->ex_slots.reset(s->slotsL, TSS_POOL_SLOT_PAGE);
     s->ex_cellsL.reset(s->CL, TSS_POOL_CELL_PAGE);
     s->ex_cellsH.reset(s->CH, TSS_POOL_CELL_PAGE);
@@ -646,6 +651,11 @@ tss_status tss_batch_create(int n_scenes, const tss_scene_desc* scenes, int cap_
     tss_status st = create_pool(c, false, &s);
     if (st != TSS_OK) return st;
     s->blocksL = (s->nL + 255) / 256;  // the low-res list is full: one block per 256 particles
+    s->low_full = true;
+    if ((st = s->apply_launch(default_launch())) != TSS_OK) {
+        delete s;
+        return st;
+    }
     // ids are handed out lowest first, so scene k gets id k
     for (int k = 0; k < n_scenes; ++k) {
         int id = -1;

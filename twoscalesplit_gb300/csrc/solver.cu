@@ -114,19 +114,61 @@ cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
     }
     if ((e = mark(3, s)) != cudaSuccess) return e;
     // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
-    launch_k_density_high(batched, blocksH, 256, s, P, V);
+    launch_k_density_high(batched, gather_grid[0], launch.threads[0], s, P, V);
     if ((e = mark(4, s)) != cudaSuccess) return e;
-    launch_k_density_low(batched, blocksL, 256, s, P, V);
+    launch_k_density_low(batched, gather_grid[1], launch.threads[1], s, P, V);
     if ((e = mark(5, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
-    launch_k_force_low(batched, blocksL, 256, s, P, V);
+    launch_k_force_low(batched, gather_grid[2], launch.threads[2], s, P, V);
     if ((e = mark(6, s)) != cudaSuccess) return e;
     launch_k_split(batched, std::min(split_ntiles, 8 * sm_count()), kSplitThreads, s, P, V);
     if ((e = mark(7, s)) != cudaSuccess) return e;
-    launch_k_force_high(batched, blocksH, 256, s, P, V);
+    launch_k_force_high(batched, gather_grid[3], launch.threads[3], s, P, V);
     k_step_finish<<<1, 32, 0, s>>>(cnt);
     if ((e = mark(8, s)) != cudaSuccess) return e;
     return cudaGetLastError();
+}
+
+// Grid of each gather for launch shape l: a covering grid is one block per
+// `threads` list entries of capacity (a full low-res list: exactly its particles;
+// otherwise at most 4096 threads per SM, striding beyond); a persistent grid is
+// one wave of resident blocks.
+tss_status tss_solver::apply_launch(const tss_launch& l) {
+    for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
+        const int t = l.threads[g];
+        if (t != 64 && t != 128 && t != 256) return fail(TSS_INVALID_ARG, "threads per block must be 64, 128 or 256");
+        if (l.persistent[g] != 0 && l.persistent[g] != 1) return fail(TSS_INVALID_ARG, "persistent must be 0 or 1");
+    }
+    const long long sms = sm_count();
+    int grid[TSS_NUM_GATHERS];
+    for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
+        const int t = l.threads[g];
+        const bool low = g == 1 || g == 2;
+        const long long cap = std::max(low ? nL : capH, 1);
+        const long long cover = (cap + t - 1) / t;
+        if (l.persistent[g]) {
+            const int occ = gather_occupancy(g, batched, t);
+            if (occ <= 0) return fail(TSS_CUDA_ERROR, "occupancy query of a gather kernel failed");
+            grid[g] = static_cast<int>(sms * occ);
+        } else if (low && low_full) {
+            grid[g] = static_cast<int>(cover);
+        } else {
+            grid[g] = static_cast<int>(std::min(cover, sms * 4096 / t));
+        }
+    }
+    launch = l;
+    for (int g = 0; g < TSS_NUM_GATHERS; ++g) gather_grid[g] = grid[g];
+    drop_graph();
+    return TSS_OK;
+}
+
+tss_launch tss::default_launch() {
+    tss_launch l{};
+    for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
+        l.threads[g] = 256;
+        l.persistent[g] = 0;
+    }
+    return l;
 }
 
 // Key pass of both grids for the current list arrays (after create or upload).
@@ -421,10 +463,16 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
     s->H.g = grid_bufs_carve(gH, cap_high > 0 ? cap_high : 1, s->CH);
     GridBufs gw = grid_bufs_carve(gW, n_wall > 0 ? n_wall : 1, s->CL);
     s->woff = gw.off;
-    // one block per 256 low-res particles (their count is fixed): every block of the
-    // gathers does one tile of work, which balances better than a capped grid-stride launch
+    // the low-res gathers take one block per 256 particles (their count is fixed):
+    // every block does one tile of work, which balances better than a capped
+    // grid-stride launch
     s->blocksL = n_low > 0 ? (n_low + 255) / 256 : 1;
     s->blocksH = particle_blocks(cap_high > 0 ? cap_high : 1, 256);
+    s->low_full = true;
+    if (s->apply_launch(default_launch()) != TSS_OK) {
+        delete s;
+        return TSS_CUDA_ERROR;
+    }
 
     if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         delete s;
@@ -483,31 +531,34 @@ void tss_solver_destroy(tss_solver* s) { delete s; }
 
 tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
     if (!s || n_steps < 0) return TSS_INVALID_ARG;
-    if (n_steps == 0) return TSS_OK;
-    cudaError_t e;
-    if (!s->exec) {
-        cudaStream_t cap = s->stream;
-        if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-            return s->cuda_fail(e, "begin capture");
-        cudaError_t e1 = s->enqueue_step(cap);
-        cudaGraph_t g = nullptr;
-        e = cudaStreamEndCapture(cap, &g);
-        if (e1 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return s->cuda_fail(e1, "enqueue step");
-        }
-        if (e != cudaSuccess) return s->cuda_fail(e, "end capture");
-        s->graph = g;
-        if ((e = cudaGraphInstantiate(&s->exec, g, 0)) != cudaSuccess) {
-            s->drop_graph();
-            return s->cuda_fail(e, "instantiate");
-        }
-    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
-    for (int k = 0; k < n_steps; ++k) {
-        if ((e = cudaGraphLaunch(s->exec, st)) != cudaSuccess) return s->cuda_fail(e, "graph launch");
-        ++s->steps_issued;
+    cudaError_t e;
+    while (n_steps > 0) {
+        int b = 0;  // bucket: 1 << b steps
+        if (!s->profile) b = n_steps >= 8 ? 3 : (n_steps >= 4 ? 2 : (n_steps >= 2 ? 1 : 0));
+        if (!s->exec[b]) {
+            cudaStream_t cap = s->stream;
+            if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                return s->cuda_fail(e, "begin capture");
+            cudaError_t e1 = cudaSuccess;
+            for (int k = 0; k < (1 << b) && e1 == cudaSuccess; ++k) e1 = s->enqueue_step(cap);
+            cudaGraph_t g = nullptr;
+            e = cudaStreamEndCapture(cap, &g);
+            if (e1 != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return s->cuda_fail(e1, "enqueue step");
+            }
+            if (e != cudaSuccess) return s->cuda_fail(e, "end capture");
+            s->graph[b] = g;
+            if ((e = cudaGraphInstantiate(&s->exec[b], g, 0)) != cudaSuccess) {
+                s->drop_graph();
+                return s->cuda_fail(e, "instantiate");
+            }
+        }
+        if ((e = cudaGraphLaunch(s->exec[b], st)) != cudaSuccess) return s->cuda_fail(e, "graph launch");
+        s->steps_issued += 1 << b;
         s->phys_low = s->live_low;  // the step's grid build dropped the retired scenes' entries
+        n_steps -= 1 << b;
     }
     s->uploaded[0] = s->uploaded[1] = false;
     return TSS_OK;
@@ -786,6 +837,73 @@ tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n) {
     cudaError_t e = cudaDeviceSynchronize();
     for (int k = 0; k < TSS_NUM_STAGES && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&ms[k], s->ev[k], s->ev[k + 1]);
     if (e != cudaSuccess) return s->cuda_fail(e, "stage times");
+    return TSS_OK;
+}
+
+tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out) {
+    if (!s || !out) return TSS_INVALID_ARG;
+    *out = s->launch;
+    return TSS_OK;
+}
+
+tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in) {
+    if (!s || !in) return TSS_INVALID_ARG;
+    cudaError_t e = cudaStreamSynchronize(s->stream);  // no capture of the old graphs in flight
+    if (e != cudaSuccess) return s->cuda_fail(e, "set launch");
+    return s->apply_launch(*in);
+}
+
+// Stage of each gather in the profiled step (tss_solver_stage_times).
+static const int kGatherStage[TSS_NUM_GATHERS] = {3, 4, 5, 7};
+
+tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* best, int* steps_taken) {
+    if (!s || !best || steps_per_trial < 1) return TSS_INVALID_ARG;
+    const bool was_profiling = s->profile;
+    const tss_launch before = s->launch;
+    tss_status st = tss_solver_profile(s, 1);
+    if (st != TSS_OK) return st;
+    tss_launch b = before;
+    float best_ms[TSS_NUM_GATHERS];
+    for (float& x : best_ms) x = 3.0e38f;
+    int taken = 0;
+    const int threads[3] = {64, 128, 256};
+    for (int pers = 0; pers < 2 && st == TSS_OK; ++pers) {
+        for (int ti = 0; ti < 3 && st == TSS_OK; ++ti) {
+            tss_launch c{};
+            for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
+                c.threads[g] = threads[ti];
+                c.persistent[g] = pers;
+            }
+            if ((st = s->apply_launch(c)) != TSS_OK) break;
+            // one untimed step captures the graph
+            if ((st = tss_solver_step(s, 1, s->stream)) != TSS_OK) break;
+            ++taken;
+            float sum[TSS_NUM_GATHERS] = {};
+            for (int k = 0; k < steps_per_trial && st == TSS_OK; ++k) {
+                if ((st = tss_solver_step(s, 1, s->stream)) != TSS_OK) break;
+                ++taken;
+                float ms[TSS_NUM_STAGES];
+                if ((st = tss_solver_stage_times(s, ms, TSS_NUM_STAGES)) != TSS_OK) break;
+                for (int g = 0; g < TSS_NUM_GATHERS; ++g) sum[g] += ms[kGatherStage[g]];
+            }
+            if (st != TSS_OK) break;
+            for (int g = 0; g < TSS_NUM_GATHERS; ++g)
+                if (sum[g] < best_ms[g]) {
+                    best_ms[g] = sum[g];
+                    b.threads[g] = c.threads[g];
+                    b.persistent[g] = c.persistent[g];
+                }
+        }
+    }
+    if (st == TSS_OK) st = tss_solver_sync(s);  // a numeric or capacity error of the trial steps
+    if (st != TSS_OK) {
+        s->apply_launch(before);
+        return st;
+    }
+    if ((st = s->apply_launch(b)) != TSS_OK) return st;
+    if ((st = tss_solver_profile(s, was_profiling ? 1 : 0)) != TSS_OK) return st;
+    *best = b;
+    if (steps_taken) *steps_taken = taken;
     return TSS_OK;
 }
 

@@ -78,6 +78,7 @@ struct SceneRec {
 };
 
 bool valid_cfg(const tss_config* cfg);
+tss_launch default_launch();  // 256 threads per block, covering grids
 Params make_params(const SceneIn& sc);
 void scene_runs(const SceneIn& sc, tss_footprint* f);  // unrounded footprint
 
@@ -110,9 +111,14 @@ struct tss_solver {
     float2* relax_pos = nullptr;
     float2* relax_vel = nullptr;
     cudaStream_t stream = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    int blocksL = 1, blocksH = 1;
+    // step graphs of 1, 2, 4 and 8 steps (bucket b holds 1 << b steps)
+    static constexpr int kBuckets = 4;
+    cudaGraph_t graph[kBuckets] = {};
+    cudaGraphExec_t exec[kBuckets] = {};
+    int blocksL = 1, blocksH = 1;           // the non-gather particle kernels
+    bool low_full = true;                   // the low-res list is always full (single scenes, batches)
+    tss_launch launch{};                    // the gathers' launch shape
+    int gather_grid[TSS_NUM_GATHERS] = {};  // blocks of each gather for that shape
     bool uploaded[2] = {false, false};  // state replaced since the last step
     bool profile = false;
     cudaEvent_t ev[TSS_NUM_STAGES + 1] = {};
@@ -160,12 +166,15 @@ struct tss_solver {
     cudaError_t mark(int k, cudaStream_t s);
     cudaError_t enqueue_step(cudaStream_t s);
     cudaError_t prime_keys(cudaStream_t s);
+    tss_status apply_launch(const tss_launch& l);  // validates, sizes the grids, drops the graphs
 
     void drop_graph() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        exec = nullptr;
-        graph = nullptr;
+        for (int b = 0; b < kBuckets; ++b) {
+            if (exec[b]) cudaGraphExecDestroy(exec[b]);
+            if (graph[b]) cudaGraphDestroy(graph[b]);
+            exec[b] = nullptr;
+            graph[b] = nullptr;
+        }
     }
 
     ~tss_solver() {

@@ -751,4 +751,32 @@ TSS_LAUNCHER(k_relax_density)
 TSS_LAUNCHER(k_relax_force)
 #undef TSS_LAUNCHER
 
+// Resident blocks per SM of gather g (0 high-res density, 1 low-res density,
+// 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error.
+int gather_occupancy(int g, bool batched, int threads) {
+    int n = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (g) {
+        case 0:
+            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_high<true>, threads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_high<false>, threads, 0);
+            break;
+        case 1:
+            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_low<true>, threads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_low<false>, threads, 0);
+            break;
+        case 2:
+            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_low<true>, threads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_low<false>, threads, 0);
+            break;
+        case 3:
+            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_high<true>, threads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_high<false>, threads, 0);
+            break;
+        default:
+            break;
+    }
+    return e == cudaSuccess ? n : 0;
+}
+
 }  // namespace tss

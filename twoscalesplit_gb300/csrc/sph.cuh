@@ -74,5 +74,8 @@ void launch_k_split(bool batched, int blocks, int threads, cudaStream_t s, const
 void launch_k_force_high(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 void launch_k_relax_density(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 void launch_k_relax_force(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+// resident blocks per SM of gather g (0 high-res density, 1 low-res density,
+// 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error
+int gather_occupancy(int g, bool batched, int threads);
 
 }  // namespace tss

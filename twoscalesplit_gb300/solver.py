@@ -123,6 +123,25 @@ class Solver:
         self._check(self.lib.tss_solver_stage_times(self.h, fptr(ms), ms.shape[0]))
         return dict(zip(_abi.STAGE_NAMES, ms.tolist()))
 
+    @property
+    def launch(self):
+        """Launch shape of the gathers: {gather: {"threads": t, "persistent": bool}}."""
+        l = _abi.TssLaunch()
+        self._check(self.lib.tss_solver_get_launch(self.h, ctypes.byref(l)))
+        return l.as_dict()
+
+    def set_launch(self, shape):
+        self._check(self.lib.tss_solver_set_launch(self.h, ctypes.byref(_abi.TssLaunch.from_dict(shape))))
+
+    def autotune(self, steps_per_trial=3):
+        """Time every candidate launch shape on this handle's own steps and install
+        the fastest per gather (tss_solver_autotune).  The trial steps advance the
+        state (results do not depend on the shape).  Returns (shape, steps taken)."""
+        l = _abi.TssLaunch()
+        n = ctypes.c_int(0)
+        self._check(self.lib.tss_solver_autotune(self.h, int(steps_per_trial), ctypes.byref(l), ctypes.byref(n)))
+        return l.as_dict(), n.value
+
     def render(self, view, point_sizes=(0.005, 0.003, 0.005), stream=None):
         """One frame (tss_solver_render): a torch CUDA tensor (height, width, 4),
         row 0 at the bottom.  `view` is (xs, ys, xe, ye, width, height)."""

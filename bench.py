@@ -3,8 +3,10 @@
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A "step" is one WCSPHSolver::AdvanceTS-equivalent step of the whole scene (grids,
-relaxation, densities, forces, splits, integration).  W warm-up steps run first;
-the scene is then reset to its initial state and exactly K steps are timed, each
+relaxation, densities, forces, splits, integration).  W warm-up steps run first,
+then the gathers' launch-shape autotuner (its trial steps are warm-up too; the
+shape changes no result); the scene is then reset to its initial state and
+exactly K steps (default 500, the 1M dam break's step count) are timed, each
 bracketed by CUDA events on the launching stream with L2 flushed (a 512 MiB write)
 between steps.  value = sum over the timed steps of the particles processed
 (n_low + n_high at each step) / device time.  e2e repeats the timed run through
@@ -754,7 +756,8 @@ def run_adaptive(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 500 plain, 1000 batch, 2000 adaptive -- the configs' step counts)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scene", default="dam_break_1m")
@@ -775,6 +778,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape of the gathers")
     ap.add_argument("--launch-cache", default=None, help="launch-shape cache file (default: the user cache)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"plain": 500, "batch": 1000, "adaptive": 2000}.get(args.workload, 200)
     if args.workload == "batch":
         run_batch(args)
     elif args.workload == "serve":

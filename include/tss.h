@@ -396,7 +396,8 @@ tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in);
  * or persistent grids) on this handle's own steps, keeps the fastest shape of each
  * gather and installs it.  The trial steps are real steps of the handle's state
  * (the shape does not change results); *steps_taken (may be NULL) receives how many
- * were taken: 6 x (steps_per_trial + 1).  Synchronises. */
+ * were taken: 6 x (steps_per_trial + 1).  A gather keeps the default shape unless a
+ * candidate is more than 5% faster on the trial steps.  Synchronises. */
 tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* best, int* steps_taken);
 
 /* Last error message of this handle (NUL-terminated, truncated to len). */

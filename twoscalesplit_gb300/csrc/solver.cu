@@ -862,38 +862,43 @@ tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* b
     const tss_launch before = s->launch;
     tss_status st = tss_solver_profile(s, 1);
     if (st != TSS_OK) return st;
-    tss_launch b = before;
+    // The default shape is timed first and a candidate replaces the incumbent of a
+    // gather only when it is faster by more than kMargin: trial steps are few and
+    // early (a scale may still be nearly empty), and a shape that wins by noise
+    // can lose once the lists fill.
+    constexpr float kMargin = 0.05f;
+    tss_launch b = default_launch();
     float best_ms[TSS_NUM_GATHERS];
     for (float& x : best_ms) x = 3.0e38f;
     int taken = 0;
-    const int threads[3] = {64, 128, 256};
-    for (int pers = 0; pers < 2 && st == TSS_OK; ++pers) {
-        for (int ti = 0; ti < 3 && st == TSS_OK; ++ti) {
-            tss_launch c{};
-            for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
-                c.threads[g] = threads[ti];
-                c.persistent[g] = pers;
-            }
-            if ((st = s->apply_launch(c)) != TSS_OK) break;
-            // one untimed step captures the graph
+    // candidates in order: the default (256 threads, covering) first
+    const int cand_threads[6] = {256, 128, 64, 256, 128, 64};
+    const int cand_pers[6] = {0, 0, 0, 1, 1, 1};
+    for (int ci = 0; ci < 6 && st == TSS_OK; ++ci) {
+        tss_launch c{};
+        for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
+            c.threads[g] = cand_threads[ci];
+            c.persistent[g] = cand_pers[ci];
+        }
+        if ((st = s->apply_launch(c)) != TSS_OK) break;
+        // one untimed step captures the graph
+        if ((st = tss_solver_step(s, 1, s->stream)) != TSS_OK) break;
+        ++taken;
+        float sum[TSS_NUM_GATHERS] = {};
+        for (int k = 0; k < steps_per_trial && st == TSS_OK; ++k) {
             if ((st = tss_solver_step(s, 1, s->stream)) != TSS_OK) break;
             ++taken;
-            float sum[TSS_NUM_GATHERS] = {};
-            for (int k = 0; k < steps_per_trial && st == TSS_OK; ++k) {
-                if ((st = tss_solver_step(s, 1, s->stream)) != TSS_OK) break;
-                ++taken;
-                float ms[TSS_NUM_STAGES];
-                if ((st = tss_solver_stage_times(s, ms, TSS_NUM_STAGES)) != TSS_OK) break;
-                for (int g = 0; g < TSS_NUM_GATHERS; ++g) sum[g] += ms[kGatherStage[g]];
-            }
-            if (st != TSS_OK) break;
-            for (int g = 0; g < TSS_NUM_GATHERS; ++g)
-                if (sum[g] < best_ms[g]) {
-                    best_ms[g] = sum[g];
-                    b.threads[g] = c.threads[g];
-                    b.persistent[g] = c.persistent[g];
-                }
+            float ms[TSS_NUM_STAGES];
+            if ((st = tss_solver_stage_times(s, ms, TSS_NUM_STAGES)) != TSS_OK) break;
+            for (int g = 0; g < TSS_NUM_GATHERS; ++g) sum[g] += ms[kGatherStage[g]];
         }
+        if (st != TSS_OK) break;
+        for (int g = 0; g < TSS_NUM_GATHERS; ++g)
+            if (ci == 0 || sum[g] < (1.0f - kMargin) * best_ms[g]) {
+                best_ms[g] = sum[g];
+                b.threads[g] = c.threads[g];
+                b.persistent[g] = c.persistent[g];
+            }
     }
     if (st == TSS_OK) st = tss_solver_sync(s);  // a numeric or capacity error of the trial steps
     if (st != TSS_OK) {

@@ -550,8 +550,11 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     }
 }
 
+// The batched form reads each particle's parameters from the scene table; at 40
+// registers it spills ~300 bytes, at 48 (five blocks per SM) a third of that, which
+// measured 5 % faster on the mixed batch (the single-scene form keeps six blocks).
 template <bool B>
-__global__ void __launch_bounds__(256, 6) k_force_high(Params P0, StepView V) {
+__global__ void __launch_bounds__(256, B ? 5 : 6) k_force_high(Params P0, StepView V) {
     const int n = V.cnt->cur[1];
     for (int i = tid(); i < n; i += nthreads()) {
         if constexpr (B) {

@@ -80,9 +80,14 @@ class Pool(Batch):
         self.h = h
 
     def can_admit(self, scene):
+        """True if the pool has room for the scene now, False if not (TSS_CAPACITY)."""
         keep = []
         d = scene_desc(scene, keep)
-        return self.lib.tss_pool_can_admit(self.h, ctypes.byref(d))
+        st = self.lib.tss_pool_can_admit(self.h, ctypes.byref(d))
+        if st == _abi.TSS_CAPACITY:
+            return False
+        self._check(st)
+        return True
 
     def admit(self, scene, stream=None):
         """Scene id, or None when the pool has no room now (TSS_CAPACITY)."""

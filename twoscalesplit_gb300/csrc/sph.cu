@@ -48,7 +48,7 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
             });
             if (j < 0) break;
             const float dist = sqrtf(x);
-            d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            d += pair_density(P, dist);
         }
     }
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
@@ -81,7 +81,7 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
                 const float x = sq(sub(p, pj));
                 if (x <= P.Tle_rh) {
                     const float dist = sqrtf(x);
-                    d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+                    d += pair_density(P, dist);
                 }
             }
         }
@@ -96,7 +96,7 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
             });
             if (j < 0) break;
             const float dist = sqrtf(x);
-            dl += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            dl += pair_density(P, dist);
         }
     }
     d *= P.mH;
@@ -144,7 +144,7 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
             });
             if (j < 0) break;
             const float dist = sqrtf(x);
-            d += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            d += pair_density(P, dist);
         }
     }
     if (cross) {  // only state-0 high-res particles can contribute (lambda_LH)
@@ -160,7 +160,7 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
             });
             if (j < 0) break;
             const float dist = sqrtf(x);
-            dh += (kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH)) / 2.0f;
+            dh += pair_density(P, dist);
         }
     }
     d *= P.mL;
@@ -217,6 +217,7 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
 // accumulators, so they are taken in two passes over the window.  The new position
 // also gives the entry's key for the next step's grid.  Returns the split flag.
 // ---------------------------------------------------------------------------
+template <bool B>
 __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V, int i, bool cross) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
@@ -238,7 +239,7 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
                 return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
             });
             if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
+            pair_force<!B>(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
         }
     }
     const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
@@ -256,7 +257,7 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
                 return x != 0.0f && x <= P.Tlt_r;
             });
             if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
+            pair_force<!B>(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
         }
     }
     acc.x *= -P.mL;
@@ -308,8 +309,10 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
 // Warp-uniform loop: every lane makes the same number of trips (lanes past n are
 // inactive) so the ballot that feeds the split compaction sees whole warps; a
 // warp's 32 particles lie in one compaction tile (kSplitTile % 32 == 0).
+// Register budgets measured per form: the single-scene form (packed kernel pairs)
+// at 48 registers (five blocks per SM), the batched form at 40 (six).
 template <bool B>
-__global__ void __launch_bounds__(256, 6) k_force_low(Params P0, StepView V) {
+__global__ void __launch_bounds__(256, B ? 6 : 5) k_force_low(Params P0, StepView V) {
     const int n = V.cnt->cur[0];
     const bool cross = V.cnt->h_state0 != 0;
     const int lane = threadIdx.x & 31;
@@ -319,9 +322,9 @@ __global__ void __launch_bounds__(256, 6) k_force_low(Params P0, StepView V) {
         if (i < n) {
             if constexpr (B) {
                 const Params P = V.table[V.scL[i]];
-                flag = force_low_one(P, V, i, cross);
+                flag = force_low_one<true>(P, V, i, cross);
             } else {
-                flag = force_low_one(P0, V, i, cross);
+                flag = force_low_one<false>(P0, V, i, cross);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, flag);
@@ -371,6 +374,9 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) 
     const int capH = P0.capH;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        // k_force_low counted this tile's flags: a tile without a split has nothing
+        // to compact (only the last tile is always taken: it publishes the counts)
+        if (tile != ntiles - 1 && V.split_tile[tile] == 0u) continue;
         unsigned before = 0;
         for (int t = threadIdx.x; t < tile; t += blockDim.x) before += V.split_tile[t];
 #pragma unroll
@@ -450,6 +456,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) 
 // Reads see the pre-step state (the reference integrates in place, a data race);
 // low-res states are read after this step's split marks, as in the reference.
 // ---------------------------------------------------------------------------
+template <bool B>
 __device__ __forceinline__ void force_high_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
@@ -472,7 +479,7 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
                 return x != 0.0f && x <= P.Tlt_rh;
             });
             if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
+            pair_force<!B>(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
         }
     }
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
@@ -490,7 +497,7 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
                 return x != 0.0f && x <= P.Tlt_r;
             });
             if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
+            pair_force<!B>(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
         }
     }
     const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
@@ -559,9 +566,9 @@ __global__ void __launch_bounds__(256, B ? 5 : 6) k_force_high(Params P0, StepVi
     for (int i = tid(); i < n; i += nthreads()) {
         if constexpr (B) {
             const Params P = V.table[V.scH[i]];
-            force_high_one(P, V, i);
+            force_high_one<true>(P, V, i);
         } else {
-            force_high_one(P0, V, i);
+            force_high_one<false>(P0, V, i);
         }
     }
 }

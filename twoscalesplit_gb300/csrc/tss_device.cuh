@@ -65,9 +65,13 @@ struct Counters {
 __device__ __forceinline__ int f2i(float v) { return static_cast<int>(v); }  // cvt.rzi: trunc, saturating
 
 // Packed FP32 pairs: sm_100's two-wide add and multiply (__fadd2_rn, __fmul2_rn)
-// round each component exactly as __fadd_rn / __fmul_rn do, which are never merged
-// into a multiply-add, so packing the x and y halves of an expression changes no
-// result.  a - b is a + (-b) (IEEE defines subtraction so).
+// round each component exactly as the scalar operation.  --fmad=false keeps the
+// scalar multiplies and adds apart, but not the packed ones: a packed product used
+// once and fed to a packed add or subtract was measured to come out as one packed
+// fused multiply-add.  So no packed product here feeds a packed add or subtract
+// directly, except an exact product (by 0.5, where fusing changes nothing); such
+// a difference is taken in scalar, and the parity tests pin every result to the
+// scalar expression bit for bit.  a - b is a + (-b) (IEEE defines subtraction so).
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -110,6 +114,46 @@ __device__ __forceinline__ float2 kernDW(float2 x, float d, float rad, float G) 
     return q < 2.0f ? mul2(make_float2(c, c), x) : make_float2(0.0f, 0.0f);
 }
 
+// Both scales' kernels at one distance d, packed in pairs: x is the low-res scale
+// (r, CL, GL), y the high-res scale (rh, CH, GH).  Each half is the scalar
+// expression of kernW / kernDW above -- the same operations in the same
+// association ((a*a)*a, ((4*b)*b)*b, ((C*a)*a)*a, (G*a)*a), each rounded once --
+// so each half equals the scalar value bit for bit.
+struct Kern2 {
+    float2 q, a, b, aa, fbb;  // q = 2d/rad, a = 2 - q, b = 1 - q, a*a, (4*b)*b
+};
+
+__device__ __forceinline__ Kern2 kern2(float d, const Params& P) {
+    Kern2 k;
+    const float d2 = d * 2.0f;
+    k.q = make_float2(d2 / P.r, d2 / P.rh);
+    k.a = sub2(make_float2(2.0f, 2.0f), k.q);
+    k.b = sub2(make_float2(1.0f, 1.0f), k.q);
+    k.aa = mul2(k.a, k.a);
+    k.fbb = mul2(mul2(make_float2(4.0f, 4.0f), k.b), k.b);
+    return k;
+}
+
+// evaluateM4Kernel of both scales: C * (a*a*a - 4*b*b*b) for q < 1, C*a*a*a for q < 2
+// (the difference of the two products in scalar: see add2 above)
+__device__ __forceinline__ float2 kernW2(const Kern2& k, float2 C) {
+    const float2 a3 = mul2(k.aa, k.a), b3 = mul2(k.fbb, k.b);
+    const float2 w1 = mul2(C, make_float2(a3.x - b3.x, a3.y - b3.y));
+    const float2 w2 = mul2(mul2(mul2(C, k.a), k.a), k.a);
+    return make_float2(k.q.x < 1.0f ? w1.x : (k.q.x < 2.0f ? w2.x : 0.0f),
+                       k.q.y < 1.0f ? w1.y : (k.q.y < 2.0f ? w2.y : 0.0f));
+}
+
+// evaluateGradientM4Kernel of both scales applied to x: gI (low-res), gJ (high-res)
+__device__ __forceinline__ void kernDW2(const Kern2& k, float2 G, float2 x, float d, float2& gI, float2& gJ) {
+    const float2 n1 = mul2(G, make_float2(k.aa.x - k.fbb.x, k.aa.y - k.fbb.y));
+    const float2 n2 = mul2(mul2(G, k.a), k.a);
+    const float cI = (k.q.x < 1.0f ? n1.x : n2.x) / d;
+    const float cJ = (k.q.y < 1.0f ? n1.y : n2.y) / d;
+    gI = k.q.x < 2.0f ? mul2(make_float2(cI, cI), x) : make_float2(0.0f, 0.0f);
+    gJ = k.q.y < 2.0f ? mul2(make_float2(cJ, cJ), x) : make_float2(0.0f, 0.0f);
+}
+
 // evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114 (selected, as above)
 __device__ __forceinline__ float wall_weight(float d, float rad, float cs) {
     const float q = d * 2.0f / rad;
@@ -139,6 +183,10 @@ __device__ __forceinline__ bool notDeleted(unsigned s) { return s < 2u; }       
 // One pair of a force sum: the body of updateAccCell / updateAccCellComplement /
 // updateAccCellHigh / updateAccCellComplementHigh (WCSPHSolver.cu:521-558 etc.).
 // qi, qj are p/rho^2 of the two particles (the reference's pre/dens2, prej/densj2).
+// Packed: both scales' kernels as float2 pairs (kern2); otherwise one scale at a
+// time (the batched kernels: fewer live registers beside the scene's parameters).
+// Both forms give the same bits.
+template <bool Packed>
 __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float dist, float2 vij, float qi, float qj,
                                            float densi, float densj, float h, float2& acc, float2& accT) {
     const float2 vp = mul2(vij, pij);
@@ -146,14 +194,30 @@ __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float di
     const float visc = dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
     float coeff = qi + qj;
     coeff = dvp < 0.0f ? coeff - visc : coeff;  // the reference's `if (dvp < 0) coeff -= ...`
-    float2 gI = kernDW(pij, dist, P.r, P.GL);
-    float2 gJ = kernDW(pij, dist, P.rh, P.GH);
+    float2 gI, gJ;
+    float ww;
+    if constexpr (Packed) {
+        const Kern2 k = kern2(dist, P);
+        kernDW2(k, make_float2(P.GL, P.GH), pij, dist, gI, gJ);
+        const float2 w = kernW2(k, make_float2(P.CL, P.CH));
+        ww = w.x + w.y;
+    } else {
+        gI = kernDW(pij, dist, P.r, P.GL);
+        gJ = kernDW(pij, dist, P.rh, P.GH);
+        ww = kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH);
+    }
     const float2 half = make_float2(0.5f, 0.5f);  // x / 2 == x * 0.5 exactly
-    acc = add2(acc, mul2(mul2(make_float2(coeff, coeff), add2(gI, gJ)), half));
-    float w = kernW(dist, P.r, P.CL);
-    float w2 = kernW(dist, P.rh, P.CH);
-    const float ww = w + w2;
+    const float2 g = make_float2(gI.x + gJ.x, gI.y + gJ.y);  // products: added in scalar (see add2)
+    acc = add2(acc, mul2(mul2(make_float2(coeff, coeff), g), half));
     accT = add2(accT, mul2(mul2(pij, make_float2(ww, ww)), half));
+}
+
+// The density term of a pair at distance d: the symmetrised kernel
+// (W_r(d) + W_rh(d)) / 2 of computeParticleDensityPressure(High)
+// (WCSPHSolver.cu:1342-1516).
+__device__ __forceinline__ float pair_density(const Params& P, float d) {
+    const float2 w = kernW2(kern2(d, P), make_float2(P.CL, P.CH));
+    return (w.x + w.y) / 2.0f;
 }
 
 // Candidates of a cell window, row by row (cells in x order, particles in cell

@@ -19,7 +19,9 @@ over the slowest rank's time.
 
 --impl reference times the CPU restatement of the reference step (the oracle,
 FP32, OpenMP over all host threads) on the same scene; the reference itself is
-CUDA code with an OpenGL front end and has no CPU implementation of its own.
+CUDA code with an OpenGL front end and has no CPU implementation of its own.  Its
+line also carries "rebuilt_cuda": the reference's own kernels rebuilt for sm_103a
+and run on the same scene by a headless restatement of AdvanceTS.
 """
 import argparse
 import json
@@ -209,7 +211,44 @@ def run_reference(args):
                              "sample": f"{args.scene}: first {steps} of the {args.steps} requested steps from the "
                                        f"initial state, bounded to {budget:.0f} s"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["rebuilt_cuda"] = rebuilt_reference_gpu(sc, args)
     print(json.dumps(line), flush=True)
+
+
+def rebuilt_reference_gpu(sc, args, budget_s=30.0):
+    """The reference's own CUDA kernels rebuilt for sm_103a (oracle RefGPU: its
+    kernel source as a cubin, driven by a headless restatement of AdvanceTS) timed
+    on this GPU on the same scene, or why not.  Each reference step ends in its
+    three synchronous count read-backs, so the wall clock per step is its step
+    time; the run is bounded to `budget_s`."""
+    try:
+        import oracle as O
+        if not O.refgpu_available():
+            return {"unavailable": "the reference's kernels for sm_103a are not built here (no cubin or no driver)"}
+        ref = O.RefGPU(sc)
+        ref.step(max(args.warmup, 1))
+        ref = O.RefGPU(sc)  # timed from the initial state, like the other arms
+        parts, steps = 0, 0
+        t0 = time.perf_counter()
+        while steps < args.steps:
+            c = ref.counts()
+            parts += c["n_low"] + c["n_high"]
+            ref.step(1)
+            steps += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+        dt = time.perf_counter() - t0
+        c = ref.counts()
+        return {"value": parts / dt, "unit": UNIT, "ms_per_step": 1e3 * dt / steps, "steps": steps,
+                "n_high_end": c["n_high"],
+                "build": "TwoScale2D/WCSPHSolver.cu kernels (lines 14-2283) for sm_103a, nvcc -O3 with the "
+                         "reference's defaults (contraction on); texture fetches as bounded loads",
+                "split_region": "x > 0.5, hard-coded in the reference's kernels (WCSPHSolver.cu:1835), not the "
+                                "scene's region of interest",
+                "timing": "wall clock per step from the initial state, including the reference's three "
+                          "synchronous count read-backs and its thrust sorts (no rendering)"}
+    except Exception as e:  # the arm's CPU line stands without it
+        return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
 def run_ours(args):

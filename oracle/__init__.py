@@ -4,10 +4,13 @@ Python handles for
   * Oracle: the CPU restatement of the two-scale WCSPH step (tss_oracle.cpp),
     FP32 (the reference's arithmetic, bit for bit) or FP64 (error reference);
   * RefCPU: the reference's own kernel source compiled for the CPU and driven by
-    a headless harness (refcpu/), available only where the reference checkout is.
+    a headless harness (refcpu/), available only where the reference checkout is;
+  * RefGPU: the reference's own kernels compiled for sm_103a (a cubin built where
+    the checkout is) run on the GPU by a headless restatement of AdvanceTS
+    (refgpu/), for timing the reference beside the library.
 
-Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
-this package; the product (twoscalesplit_gb300) never does.
+Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg and
+reference arm import this package; the product (twoscalesplit_gb300) never does.
 """
 import ctypes
 import os
@@ -251,3 +254,80 @@ class RefCPU:
         if name in ("pos", "vel", "acc"):
             out = out.reshape(-1, 2)
         return out
+
+
+_REFGPU = None
+
+
+def _refgpu_lib():
+    global _REFGPU
+    if _REFGPU is None:
+        cubin = _build.build_refgpu_cubin()
+        if cubin is None:
+            return None
+        try:
+            lib = ctypes.CDLL(_build.build_refgpu_launcher())
+        except OSError:  # no CUDA driver on this machine
+            return None
+        vp, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        lib.refgpu_create.restype = vp
+        lib.refgpu_create.argtypes = [ctypes.c_char_p, vp, i, vp, vp, f, i, f, i, vp, f, ctypes.c_char_p, i]
+        lib.refgpu_destroy.argtypes = [vp]
+        lib.refgpu_step.restype = i
+        lib.refgpu_step.argtypes = [vp, i, ctypes.c_char_p, i]
+        lib.refgpu_counts.argtypes = [vp, vp]
+        lib.refgpu_state.restype = i
+        lib.refgpu_state.argtypes = [vp, i, vp, vp, vp, i]
+        _REFGPU = (lib, cubin)
+    return _REFGPU
+
+
+def refgpu_available():
+    return _refgpu_lib() is not None
+
+
+class RefGPU:
+    """The reference's own kernels rebuilt for sm_103a (refgpu/), run on the GPU by
+    a headless restatement of AdvanceTS; slot-indexed arrays, as the reference."""
+
+    def __init__(self, scene, cap_high=None):
+        got = _refgpu_lib()
+        if got is None:
+            raise RuntimeError("the reference's kernels for sm_103a are not built (no reference checkout)")
+        self.lib, cubin = got
+        self.scene = scene
+        lp = np.ascontiguousarray(scene.low_pos, np.float32).reshape(-1)
+        lv = None if scene.low_vel is None else np.ascontiguousarray(scene.low_vel, np.float32).reshape(-1)
+        wp = np.ascontiguousarray(scene.wall_pos, np.float32).reshape(-1)
+        err = ctypes.create_string_buffer(512)
+        self.cap_high = int(cap_high if cap_high is not None else scene.cap_high)
+        self.h = self.lib.refgpu_create(cubin.encode(), ctypes.byref(scene.config), scene.n_low, _p(lp), _p(lv),
+                                        scene.mass_low, self.cap_high, scene.mass_high, scene.n_wall, _p(wp),
+                                        scene.mass_wall, err, 512)
+        if not self.h:
+            raise RuntimeError("refgpu_create: " + err.value.decode(errors="replace"))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.refgpu_destroy(self.h)
+            self.h = None
+
+    def step(self, n=1):
+        err = ctypes.create_string_buffer(512)
+        if self.lib.refgpu_step(self.h, int(n), err, 512) != 0:
+            raise RuntimeError("refgpu_step: " + err.value.decode(errors="replace"))
+
+    def counts(self):
+        c = np.zeros(3, np.int32)
+        self.lib.refgpu_counts(self.h, _p(c))
+        return {"n_low": int(c[0]), "n_high": int(c[1]), "n_transient_low": int(c[2])}
+
+    def state(self, scale):
+        """Slot-indexed positions, velocities and states of a scale (capacity-sized)."""
+        cap = self.scene.n_low if scale == 0 else self.cap_high
+        pos = np.zeros((max(cap, 1), 2), np.float32)
+        vel = np.zeros((max(cap, 1), 2), np.float32)
+        st = np.zeros(max(cap, 1), np.uint8)
+        if self.lib.refgpu_state(self.h, scale, _p(pos), _p(vel), _p(st), cap) != 0:
+            raise RuntimeError("refgpu_state failed")
+        return pos[:cap], vel[:cap], st[:cap]

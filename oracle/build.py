@@ -6,6 +6,12 @@
   _ref/librefcpu.so   -- the reference's own kernel source compiled for the CPU
                          (refcpu/build_ref.sh); only when the reference checkout is
                          present, i.e. on the build machine, not on the GPU machine
+  _ref/refkern.cubin  -- the reference's own kernel source compiled for sm_103a
+                         (refgpu/build_refgpu.sh); only where the checkout is
+                         present.  Device code only: it travels to the GPU machine.
+  librefgpu.so        -- refgpu/refgpu_launcher.cu, the host side that loads that
+                         cubin and runs the reference's step on the GPU (nvcc;
+                         built wherever nvcc is, including the GPU machine)
 """
 import os
 import subprocess
@@ -14,6 +20,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REFCPU_SO = os.path.join(HERE, "_ref", "librefcpu.so")
+REFGPU_CUBIN = os.path.join(HERE, "_ref", "refkern.cubin")
+REFGPU_SO = os.path.join(HERE, "librefgpu.so")
 REFERENCE_ROOT = os.environ.get("TSS_REFERENCE_ROOT", "/root/reference")
 
 
@@ -47,9 +55,40 @@ def build_refcpu(force=False):
     return REFCPU_SO
 
 
+def build_refgpu_cubin(force=False):
+    """Returns the cubin path, or None when the reference sources are absent (the
+    cubin built on the build machine is then used if it is there)."""
+    cur = os.path.join(REFERENCE_ROOT, "TwoScale2D", "WCSPHSolver.cu")
+    if not os.path.exists(cur):
+        return REFGPU_CUBIN if os.path.exists(REFGPU_CUBIN) else None
+    deps = [os.path.join(HERE, "refgpu", f) for f in ("refgpu_shim.cuh", "refgpu_entry.inc", "build_refgpu.sh")]
+    if not force and not _stale(REFGPU_CUBIN, deps):
+        return REFGPU_CUBIN
+    subprocess.check_call(["sh", os.path.join(HERE, "refgpu", "build_refgpu.sh"), REFERENCE_ROOT])
+    return REFGPU_CUBIN
+
+
+def build_refgpu_launcher(force=False):
+    """Returns the launcher library path (nvcc; links the CUDA driver library)."""
+    src = os.path.join(HERE, "refgpu", "refgpu_launcher.cu")
+    hdr = os.path.join(HERE, "..", "include", "tss.h")
+    if not force and not _stale(REFGPU_SO, [src, hdr]):
+        return REFGPU_SO
+    sys.path.insert(0, os.path.join(HERE, ".."))
+    from twoscalesplit_gb300 import build as tb
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(tb.nvcc())), "lib64")
+    cmd = [tb.nvcc(), "-std=c++17", "-O2", f"-gencode=arch=compute_{tb.ARCH},code=sm_{tb.ARCH}",
+           "-Xcompiler", "-fPIC", "-shared", "-I", os.path.join(HERE, "..", "include"), "-o", REFGPU_SO, src,
+           "-L", cuda_lib, "-L", os.path.join(cuda_lib, "stubs"), "-lcuda"]
+    subprocess.check_call(cmd)
+    return REFGPU_SO
+
+
 def build(force=False):
     build_oracle(force)
     build_refcpu(force)
+    build_refgpu_cubin(force)
+    build_refgpu_launcher(force)
 
 
 if __name__ == "__main__":

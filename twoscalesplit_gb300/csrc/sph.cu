@@ -10,7 +10,9 @@
 //
 // Each kernel's per-particle work is an inlined function of the particle's Params:
 // the kernel's own constants for a single scene, the scene's table row for a
-// batch.  A scene's cell windows index its grid at its cell base in the global
+// batch.  The row is read through a reference, so each field is loaded where it is
+// used: a copy of the whole row kept every field live in registers across the
+// neighbour loops, and the batched gathers spilled and ran 5 % slower.  A scene's cell windows index its grid at its cell base in the global
 // cell space, so one sort and one offset table serve all scenes of a batch.
 #include "sph.cuh"
 
@@ -114,7 +116,7 @@ __global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
     const int n = V.cnt->cur[1];
     for (int i = tid(); i < n; i += nthreads()) {
         if constexpr (B) {
-            const Params P = V.table[V.scH[i]];
+            const Params& P = V.table[V.scH[i]];
             density_high_one(P, V, i);
         } else {
             density_high_one(P0, V, i);
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(256) k_density_low(Params P0, StepView V) {
     const bool cross = V.cnt->h_state0 != 0;
     for (int i = tid(); i < n; i += nthreads()) {
         if constexpr (B) {
-            const Params P = V.table[V.scL[i]];
+            const Params& P = V.table[V.scL[i]];
             density_low_one(P, V, i, cross);
         } else {
             density_low_one(P0, V, i, cross);
@@ -217,7 +219,6 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
 // accumulators, so they are taken in two passes over the window.  The new position
 // also gives the entry's key for the next step's grid.  Returns the split flag.
 // ---------------------------------------------------------------------------
-template <bool B>
 __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V, int i, bool cross) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
@@ -239,7 +240,7 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
                 return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
             });
             if (j < 0) break;
-            pair_force<!B>(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
+            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
         }
     }
     const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
@@ -257,7 +258,7 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
                 return x != 0.0f && x <= P.Tlt_r;
             });
             if (j < 0) break;
-            pair_force<!B>(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
+            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
         }
     }
     acc.x *= -P.mL;
@@ -309,8 +310,8 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
 // Warp-uniform loop: every lane makes the same number of trips (lanes past n are
 // inactive) so the ballot that feeds the split compaction sees whole warps; a
 // warp's 32 particles lie in one compaction tile (kSplitTile % 32 == 0).
-// Register budgets measured per form: the single-scene form (packed kernel pairs)
-// at 48 registers (five blocks per SM), the batched form at 40 (six).
+// Register budgets measured per form: the single-scene form at 48 registers (five
+// blocks per SM), the batched form at 40 (six).
 template <bool B>
 __global__ void __launch_bounds__(256, B ? 6 : 5) k_force_low(Params P0, StepView V) {
     const int n = V.cnt->cur[0];
@@ -321,10 +322,10 @@ __global__ void __launch_bounds__(256, B ? 6 : 5) k_force_low(Params P0, StepVie
         bool flag = false;
         if (i < n) {
             if constexpr (B) {
-                const Params P = V.table[V.scL[i]];
-                flag = force_low_one<true>(P, V, i, cross);
+                const Params& P = V.table[V.scL[i]];
+                flag = force_low_one(P, V, i, cross);
             } else {
-                flag = force_low_one<false>(P0, V, i, cross);
+                flag = force_low_one(P0, V, i, cross);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, flag);
@@ -436,7 +437,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) 
                     const long long hb = static_cast<long long>(nH) + 4LL * r;
                     if (hb + 4 <= capH) {
                         if constexpr (B) {
-                            const Params P = V.table[V.scL[i]];
+                            const Params& P = V.table[V.scL[i]];
                             make_children(P, V, i, id, hb);
                         } else {
                             make_children(P0, V, i, id, hb);
@@ -456,7 +457,6 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) 
 // Reads see the pre-step state (the reference integrates in place, a data race);
 // low-res states are read after this step's split marks, as in the reference.
 // ---------------------------------------------------------------------------
-template <bool B>
 __device__ __forceinline__ void force_high_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
@@ -479,7 +479,7 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
                 return x != 0.0f && x <= P.Tlt_rh;
             });
             if (j < 0) break;
-            pair_force<!B>(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
+            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
         }
     }
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
@@ -497,7 +497,7 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
                 return x != 0.0f && x <= P.Tlt_r;
             });
             if (j < 0) break;
-            pair_force<!B>(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
+            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
         }
     }
     const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
@@ -565,10 +565,10 @@ __global__ void __launch_bounds__(256, B ? 5 : 6) k_force_high(Params P0, StepVi
     const int n = V.cnt->cur[1];
     for (int i = tid(); i < n; i += nthreads()) {
         if constexpr (B) {
-            const Params P = V.table[V.scH[i]];
-            force_high_one<true>(P, V, i);
+            const Params& P = V.table[V.scH[i]];
+            force_high_one(P, V, i);
         } else {
-            force_high_one<false>(P0, V, i);
+            force_high_one(P0, V, i);
         }
     }
 }
@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(256) k_relax_density(Params P0, StepView V) {
         const int i = fresh_child(P0, V, f);
         if (i < 0) continue;
         if constexpr (B) {
-            const Params P = V.table[V.scH[i]];
+            const Params& P = V.table[V.scH[i]];
             relax_density_one(P, V, i);
         } else {
             relax_density_one(P0, V, i);
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(256) k_relax_force(Params P0, StepView V) {
         const int i = fresh_child(P0, V, f);
         if (i < 0) continue;
         if constexpr (B) {
-            const Params P = V.table[V.scH[i]];
+            const Params& P = V.table[V.scH[i]];
             relax_force_one(P, V, i, f);
         } else {
             relax_force_one(P0, V, i, f);

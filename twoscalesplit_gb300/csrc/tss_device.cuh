@@ -183,10 +183,7 @@ __device__ __forceinline__ bool notDeleted(unsigned s) { return s < 2u; }       
 // One pair of a force sum: the body of updateAccCell / updateAccCellComplement /
 // updateAccCellHigh / updateAccCellComplementHigh (WCSPHSolver.cu:521-558 etc.).
 // qi, qj are p/rho^2 of the two particles (the reference's pre/dens2, prej/densj2).
-// Packed: both scales' kernels as float2 pairs (kern2); otherwise one scale at a
-// time (the batched kernels: fewer live registers beside the scene's parameters).
-// Both forms give the same bits.
-template <bool Packed>
+// Both scales' kernels are evaluated as float2 pairs (kern2).
 __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float dist, float2 vij, float qi, float qj,
                                            float densi, float densj, float h, float2& acc, float2& accT) {
     const float2 vp = mul2(vij, pij);
@@ -194,18 +191,11 @@ __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float di
     const float visc = dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
     float coeff = qi + qj;
     coeff = dvp < 0.0f ? coeff - visc : coeff;  // the reference's `if (dvp < 0) coeff -= ...`
+    const Kern2 k = kern2(dist, P);
     float2 gI, gJ;
-    float ww;
-    if constexpr (Packed) {
-        const Kern2 k = kern2(dist, P);
-        kernDW2(k, make_float2(P.GL, P.GH), pij, dist, gI, gJ);
-        const float2 w = kernW2(k, make_float2(P.CL, P.CH));
-        ww = w.x + w.y;
-    } else {
-        gI = kernDW(pij, dist, P.r, P.GL);
-        gJ = kernDW(pij, dist, P.rh, P.GH);
-        ww = kernW(dist, P.r, P.CL) + kernW(dist, P.rh, P.CH);
-    }
+    kernDW2(k, make_float2(P.GL, P.GH), pij, dist, gI, gJ);
+    const float2 w = kernW2(k, make_float2(P.CL, P.CH));
+    const float ww = w.x + w.y;
     const float2 half = make_float2(0.5f, 0.5f);  // x / 2 == x * 0.5 exactly
     const float2 g = make_float2(gI.x + gJ.x, gI.y + gJ.y);  // products: added in scalar (see add2)
     acc = add2(acc, mul2(mul2(make_float2(coeff, coeff), g), half));

@@ -83,6 +83,39 @@ def measured_traffic(stage):
     return None
 
 
+def measured_warp_instructions(stage):
+    """Warp instructions per launch of a stage's kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "warp_instructions.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#") and parts[0] == stage:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def issue_roofline(stage, launch_ms, sm_mhz):
+    """Instruction-issue roofline of a kernel: warp instructions per launch (ncu)
+    over its live launch time, against 4 warp instructions per SM per cycle."""
+    inst = measured_warp_instructions(stage)
+    if inst is None or not launch_ms or not sm_mhz:
+        return None
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    achieved = inst / (launch_ms * 1e-3)
+    peak = 4.0 * sms * sm_mhz * 1e6
+    return {"bound": "issue", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "warp inst/s",
+            "frac": achieved / peak, "warp_inst_per_launch": inst,
+            "source": "profiles/warp_instructions.txt (ncu, one launch); peak = 4 per SM per cycle at the "
+                      "median SM clock of the timed region"}
+
+
 def hbm_peak():
     try:
         with open(MEASURED_PEAKS) as f:
@@ -395,6 +428,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": top_bytes, "launch_ms": st_avg[top],
                      "step": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (step_ms * 1e-3) / 1e9,
                               "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak}},
+        "issue_roofline": issue_roofline(top, st_avg[top], (clk or {}).get("sm_mhz")),
         "stage_ms": {k: round(v, 5) for k, v in st_avg.items()},
         "e2e": {"value": parts_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / K,
                 "d2h_bytes_per_step": d2h / K},

@@ -365,6 +365,20 @@ typedef struct tss_buffers {
 } tss_buffers;
 tss_status tss_solver_device_buffers(tss_solver* s, tss_buffers* out);
 
+/* Asynchronous position read-back: enqueues on `stream` one kernel that writes the
+ * positions of both lists after the last enqueued step (list order, as
+ * tss_buffers.pos; high-res entries removed in that step are still in the list,
+ * with state 2) into page-locked host memory, and the two list lengths into
+ * counts[2] (page-locked host ints).  Entries beyond cap_low / cap_high are not
+ * written (counts still gives the full lengths).  Nothing is synchronised: the
+ * caller waits on the stream (or an event recorded after this call) before reading,
+ * and may meanwhile enqueue the next steps.  The host buffers must be page-locked
+ * (cudaHostAlloc / cudaMallocHost or registered), which the GPU writes through
+ * unified addressing; other memory is TSS_INVALID_ARG.  Replaces mapping the VBOs
+ * each frame (ParticleSystem.cpp:78-98) for a renderer that reads on the host. */
+tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low, float* host_high, int cap_high,
+                                     int* counts, void* stream);
+
 /* Stage timing.  With profiling on, the captured step graph also records a CUDA
  * event at each stage boundary; tss_solver_stage_times then returns the device time
  * (ms) of each stage of the LAST step (it synchronises).  Stages, in order:

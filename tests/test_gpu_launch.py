@@ -106,3 +106,27 @@ def test_step_buckets_equal_single_steps():
     many.step(16)   # 8 + 8
     assert many.counts()["steps"] == 29
     _assert_same(_state(one), _state(many))
+
+
+def test_read_positions_equals_download_and_refuses_pageable_memory():
+    import torch
+    sc = _scene(seed=13, relax=0)
+    sol = Solver.from_scene(sc)
+    sol.step(25)
+    n_high = sol.counts()["n_high"]
+    assert n_high > 0
+    low = torch.zeros((sc.n_low, 2), dtype=torch.float32).pin_memory()
+    high = torch.zeros((sc.cap_high, 2), dtype=torch.float32).pin_memory()
+    counts = torch.zeros(2, dtype=torch.int32).pin_memory()
+    stream = torch.cuda.current_stream().cuda_stream
+    sol.read_positions(low, high, counts, stream=stream)
+    torch.cuda.synchronize()
+    assert counts.tolist() == [sc.n_low, n_high]
+    assert np.array_equal(low.numpy(), sol.download(TSS_SCALE_LOW)["pos"])
+    assert np.array_equal(high.numpy()[:n_high], sol.download(TSS_SCALE_HIGH)["pos"])
+    short = torch.zeros((3, 2), dtype=torch.float32).pin_memory()  # entries past the capacity are not written
+    sol.read_positions(short, high, counts, stream=stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(short.numpy(), low.numpy()[:3])
+    with pytest.raises(TssError):
+        sol.read_positions(torch.zeros((sc.n_low, 2), dtype=torch.float32), high, counts, stream=stream)

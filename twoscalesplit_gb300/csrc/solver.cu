@@ -208,6 +208,22 @@ __global__ void k_set_counts(Counters* c, int nL, int nH) {
 }
 __global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
 
+// Positions of both lists and their lengths into caller memory (page-locked host
+// memory for tss_solver_read_positions).
+__global__ void k_read_positions(const float2* __restrict__ lowp, const float2* __restrict__ highp,
+                                 const Counters* __restrict__ c, float2* out_low, int cap_low, float2* out_high,
+                                 int cap_high, int* counts) {
+    const int nl = c->cur[0], nh = c->cur[1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[0] = nl;
+        counts[1] = nh;
+    }
+    const int ml = min(nl, cap_low), mh = min(nh, cap_high);
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ml; i += stride) out_low[i] = lowp[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < mh; i += stride) out_high[i] = highp[i];
+}
+
 // Key pass of a pool's list: each entry's parameters come from the scene owning
 // its slot's page.
 __global__ void k_keys_batched(const float2* __restrict__ pos, const int32_t* __restrict__ id,
@@ -838,6 +854,31 @@ tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n) {
     for (int k = 0; k < TSS_NUM_STAGES && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&ms[k], s->ev[k], s->ev[k + 1]);
     if (e != cudaSuccess) return s->cuda_fail(e, "stage times");
     return TSS_OK;
+}
+
+tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low, float* host_high, int cap_high,
+                                     int* counts, void* stream) {
+    if (!s || !counts || cap_low < 0 || cap_high < 0 || (cap_low > 0 && !host_low) || (cap_high > 0 && !host_high))
+        return TSS_INVALID_ARG;
+    // the device-side addresses of the page-locked buffers (an error for memory the
+    // GPU cannot reach, which is refused before any kernel touches it)
+    void* dev[3] = {nullptr, nullptr, nullptr};
+    void* host[3] = {host_low, host_high, counts};
+    for (int k = 0; k < 3; ++k) {
+        if (!host[k]) continue;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, host[k]) != cudaSuccess || a.type != cudaMemoryTypeHost ||
+            cudaHostGetDevicePointer(&dev[k], host[k], 0) != cudaSuccess || !dev[k]) {
+            cudaGetLastError();  // clear the failed query
+            return s->fail(TSS_INVALID_ARG, "read_positions: host buffers must be page-locked and mapped");
+        }
+    }
+    const int blocks = std::max(1, std::min(particle_blocks(std::max(cap_low, cap_high), 256), 4 * sm_count()));
+    k_read_positions<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        s->L.npos, s->H.npos, s->cnt, static_cast<float2*>(dev[0]), cap_low, static_cast<float2*>(dev[1]),
+        cap_high, static_cast<int*>(dev[2]));
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TSS_OK : s->cuda_fail(e, "read_positions");
 }
 
 tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out) {

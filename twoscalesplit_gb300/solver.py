@@ -123,6 +123,16 @@ class Solver:
         self._check(self.lib.tss_solver_stage_times(self.h, fptr(ms), ms.shape[0]))
         return dict(zip(_abi.STAGE_NAMES, ms.tolist()))
 
+    def read_positions(self, host_low, host_high, counts, stream=None):
+        """Enqueue the asynchronous position read-back (tss_solver_read_positions)
+        into page-locked torch CPU tensors: host_low (cap_low, 2) and host_high
+        (cap_high, 2) float32, counts (2,) int32.  Wait on the stream (or an event
+        recorded after it) before reading them."""
+        self._check(self.lib.tss_solver_read_positions(
+            self.h, ctypes.c_void_p(host_low.data_ptr()), int(host_low.shape[0]),
+            ctypes.c_void_p(host_high.data_ptr()), int(host_high.shape[0]), ctypes.c_void_p(counts.data_ptr()),
+            ctypes.c_void_p(stream) if stream else None))
+
     @property
     def launch(self):
         """Launch shape of the gathers: {gather: {"threads": t, "persistent": bool}}."""

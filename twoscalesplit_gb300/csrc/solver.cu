@@ -889,7 +889,8 @@ tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out) {
 
 tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in) {
     if (!s || !in) return TSS_INVALID_ARG;
-    cudaError_t e = cudaStreamSynchronize(s->stream);  // no capture of the old graphs in flight
+    // steps run on callers' streams: wait for all of them before the old graphs go
+    cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return s->cuda_fail(e, "set launch");
     return s->apply_launch(*in);
 }
@@ -943,7 +944,10 @@ tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* b
     }
     if (st == TSS_OK) st = tss_solver_sync(s);  // a numeric or capacity error of the trial steps
     if (st != TSS_OK) {
+        const std::string why = s->err;
         s->apply_launch(before);
+        tss_solver_profile(s, was_profiling ? 1 : 0);
+        s->err = why;
         return st;
     }
     if ((st = s->apply_launch(b)) != TSS_OK) return st;

@@ -211,7 +211,9 @@ def tuned_shape(sol, kind, n_low, args):
 
 
 def compact_shape(shape):
-    return {g: f"{v['threads']}{'p' if v['persistent'] else ''}" for g, v in shape.items()}
+    """threads per block, 'p' for a persistent grid, 'w' for one particle per warp"""
+    return {g: f"{v['threads']}{'p' if v['persistent'] else ''}{'w' if v.get('per_warp') else ''}"
+            for g, v in shape.items()}
 
 
 def run_reference(args):

@@ -398,20 +398,25 @@ tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n);
  * list (WCSPHSolver.cu:2421,2437); that shape is the default here. */
 #define TSS_NUM_GATHERS 4
 typedef struct tss_launch {
-    int threads[TSS_NUM_GATHERS];     /* threads per block: 64, 128 or 256 (one particle per thread) */
+    int threads[TSS_NUM_GATHERS];     /* threads per block: 64, 128 or 256                          */
     int persistent[TSS_NUM_GATHERS];  /* 0: blocks cover the list's capacity (at most 4096 threads
                                          per SM, grid-striding beyond); 1: one wave of resident
                                          blocks (SMs x blocks per SM), each striding over the list */
+    int per_warp[TSS_NUM_GATHERS];    /* 0: one particle per thread (32 per warp); 1: one particle
+                                         per warp, its candidates spread over the lanes (for
+                                         scenes too small to fill the GPU)                         */
 } tss_launch;
 tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out);
 /* Replaces the launch shape (the step graphs are captured again at the next step). */
 tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in);
 /* Launch-shape autotuner: times every candidate shape (threads 64/128/256, covering
- * or persistent grids) on this handle's own steps, keeps the fastest shape of each
+ * or persistent grids, one particle per thread; and one particle per warp) on this
+ * handle's own steps, keeps the fastest shape of each
  * gather and installs it.  The trial steps are real steps of the handle's state
  * (the shape does not change results); *steps_taken (may be NULL) receives how many
- * were taken: 6 x (steps_per_trial + 1).  A gather keeps the default shape unless a
- * candidate is more than 5% faster on the trial steps.  Synchronises. */
+ * were taken: 7 x (steps_per_trial + 1) (six per-thread shapes and one per-warp).  A
+ * gather keeps the default shape unless a candidate is more than 5% faster on the
+ * trial steps.  Synchronises. */
 tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* best, int* steps_taken);
 
 /* Last error message of this handle (NUL-terminated, truncated to len). */

@@ -92,8 +92,9 @@ def test_launch_struct_layout_and_argument_checks(lib, tmp_path):
                            "-o", str(exe)])
     size, off = map(int, subprocess.check_output([str(exe)]).split())
     assert size == ctypes.sizeof(_abi.TssLaunch) and off == _abi.TssLaunch.persistent.offset
-    shape = {g: {"threads": t, "persistent": p} for g, t, p in zip(_abi.GATHER_NAMES, (64, 128, 256, 64),
-                                                                      (True, False, False, True))}
+    shape = {g: {"threads": t, "persistent": p, "per_warp": w}
+             for g, t, p, w in zip(_abi.GATHER_NAMES, (64, 128, 256, 64), (True, False, False, True),
+                                   (False, True, False, True))}
     assert _abi.TssLaunch.from_dict(shape).as_dict() == shape
     l = _abi.TssLaunch()
     assert lib.tss_solver_get_launch(None, ctypes.byref(l)) == _abi.TSS_INVALID_ARG

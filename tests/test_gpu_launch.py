@@ -37,8 +37,8 @@ def _assert_same(a, b):
             assert np.array_equal(sa[name], sb[name]), name
 
 
-def _shape(threads, persistent):
-    return {g: {"threads": threads, "persistent": persistent} for g in GATHER_NAMES}
+def _shape(threads, persistent, per_warp=False):
+    return {g: {"threads": threads, "persistent": persistent, "per_warp": per_warp} for g in GATHER_NAMES}
 
 
 def test_default_shape_is_the_reference_block_size():
@@ -46,13 +46,14 @@ def test_default_shape_is_the_reference_block_size():
     assert sol.launch == _shape(256, False)
 
 
-@pytest.mark.parametrize("threads,persistent", list(itertools.product([64, 128, 256], [False, True])))
-def test_every_shape_gives_the_same_steps(threads, persistent):
+@pytest.mark.parametrize("threads,persistent,per_warp",
+                         list(itertools.product([64, 128, 256], [False, True], [False, True])))
+def test_every_shape_gives_the_same_steps(threads, persistent, per_warp):
     sc = _scene()
     ref = Solver.from_scene(sc)
     ref.step(60)
     sol = Solver.from_scene(sc)
-    sol.set_launch(_shape(threads, persistent))
+    sol.set_launch(_shape(threads, persistent, per_warp))
     sol.step(60)
     sol.sync()
     assert sol.counts()["n_high"] > 0
@@ -62,8 +63,9 @@ def test_every_shape_gives_the_same_steps(threads, persistent):
 def test_shape_of_a_batch_does_not_change_its_scenes():
     scs = [_scene(seed=s, relax=0) for s in (5, 6, 7)]
     a, b = Batch(scs), Batch(scs)
-    mixed = {g: {"threads": t, "persistent": p} for g, t, p in zip(GATHER_NAMES, (64, 128, 256, 64),
-                                                                      (True, False, True, False))}
+    mixed = {g: {"threads": t, "persistent": p, "per_warp": w}
+             for g, t, p, w in zip(GATHER_NAMES, (64, 128, 256, 64), (True, False, True, False),
+                                   (True, True, False, True))}
     b.set_launch(mixed)
     a.step(50)
     b.step(50)
@@ -78,7 +80,7 @@ def test_autotune_installs_a_valid_shape_and_keeps_the_trajectory():
     sc = _scene(seed=11)
     tuned = Solver.from_scene(sc)
     shape, taken = tuned.autotune(steps_per_trial=2)
-    assert taken == 6 * 3
+    assert taken == 7 * 3
     assert tuned.launch == shape
     for g in GATHER_NAMES:
         assert shape[g]["threads"] in (64, 128, 256)

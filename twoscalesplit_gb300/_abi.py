@@ -169,12 +169,14 @@ class TssView(ctypes.Structure):
 
 
 class TssLaunch(ctypes.Structure):
-    """struct tss_launch: threads per block and grid kind of each gather kernel."""
-    _fields_ = [("threads", ctypes.c_int * TSS_NUM_GATHERS), ("persistent", ctypes.c_int * TSS_NUM_GATHERS)]
+    """struct tss_launch: threads per block, grid kind and particles per warp of each
+    gather kernel."""
+    _fields_ = [("threads", ctypes.c_int * TSS_NUM_GATHERS), ("persistent", ctypes.c_int * TSS_NUM_GATHERS),
+                ("per_warp", ctypes.c_int * TSS_NUM_GATHERS)]
 
     def as_dict(self):
-        return {g: {"threads": self.threads[k], "persistent": bool(self.persistent[k])}
-                for k, g in enumerate(GATHER_NAMES)}
+        return {g: {"threads": self.threads[k], "persistent": bool(self.persistent[k]),
+                    "per_warp": bool(self.per_warp[k])} for k, g in enumerate(GATHER_NAMES)}
 
     @classmethod
     def from_dict(cls, d):
@@ -182,6 +184,7 @@ class TssLaunch(ctypes.Structure):
         for k, g in enumerate(GATHER_NAMES):
             l.threads[k] = int(d[g]["threads"])
             l.persistent[k] = 1 if d[g]["persistent"] else 0
+            l.per_warp[k] = 1 if d[g].get("per_warp", False) else 0
         return l
 
 

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtss.so")
 SOURCES = ["grid.cu", "grid_noalloc.cu", "sph.cu", "solver.cu", "pool.cu", "render.cu", "serve.cpp"]
-HEADERS = ["tss_device.cuh", "grid.cuh", "sph.cuh", "solver_impl.cuh", "extent.hpp"]
+HEADERS = ["tss_device.cuh", "gather.cuh", "grid.cuh", "sph.cuh", "solver_impl.cuh", "extent.hpp"]
 ARCH = os.environ.get("TSS_CUDA_ARCH", "103a")
 
 

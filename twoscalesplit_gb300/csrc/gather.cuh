@@ -1,0 +1,87 @@
+// gather.cuh -- the two ways a gather walks one particle's cell window.
+//
+// PerThread: one particle per thread, 32 particles per warp.  Each thread walks its
+// window's candidates in order with the Window cursor and evaluates each accepted
+// pair as it finds it.  This is the throughput form: consecutive threads walk
+// overlapping windows, so neighbour loads are shared through L1.
+//
+// PerWarp: one particle per warp.  The 32 lanes test 32 consecutive candidates of
+// a row at a time and evaluate the accepted pairs' terms in parallel; then every
+// lane adds the terms in candidate order, taking each from the lane that evaluated
+// it (warp shuffles), so every lane ends with the per-thread sum, bit for bit.  For
+// scenes too small to fill the GPU, where a step is bound by each thread's chain
+// of dependent loads rather than by instruction issue.
+//
+// A gather is written once against the policy G: G::window / G::span take the
+// candidate test (which may leave state for the term, as the per-thread cursor
+// needs), the pair term, the accumulation, and the running sum.  Per-particle
+// results are stored by G::leader() only.
+#pragma once
+#include "tss_device.cuh"
+
+namespace tss {
+
+__device__ __forceinline__ float shfl_from(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float2 shfl_from(float2 v, int src) {
+    return make_float2(shfl_from(v.x, src), shfl_from(v.y, src));
+}
+__device__ __forceinline__ PairTerms shfl_from(const PairTerms& v, int src) {
+    return PairTerms{shfl_from(v.a, src), shfl_from(v.t, src)};
+}
+
+struct PerThread {
+    static constexpr bool kWarp = false;
+    __device__ __forceinline__ static bool leader() { return true; }
+
+    template <class T, class Test, class Term, class Add>
+    __device__ __forceinline__ static void window(const int* off, int dimx, int csx, int cex, int csy, int cey,
+                                                  Test&& test, Term&& term, Add&& add, T& sum) {
+        Window w(off, dimx, csx, cex, csy, cey);
+        for (;;) {
+            const int j = w.next(test);
+            if (j < 0) break;
+            add(sum, term(j));
+        }
+    }
+
+    // the candidates [a, b), in order
+    template <class T, class Test, class Term, class Add>
+    __device__ __forceinline__ static void span(int a, int b, Test&& test, Term&& term, Add&& add, T& sum) {
+        for (int k = a; k < b; ++k)
+            if (test(k)) add(sum, term(k));
+    }
+};
+
+struct PerWarp {
+    static constexpr bool kWarp = true;
+    __device__ __forceinline__ static bool leader() { return (threadIdx.x & 31u) == 0u; }
+
+    // a and b are the same in every lane (one particle per warp)
+    template <class T, class Test, class Term, class Add>
+    __device__ __forceinline__ static void span(int a, int b, Test&& test, Term&& term, Add&& add, T& sum) {
+        const int lane = static_cast<int>(threadIdx.x & 31u);
+        for (int base = a; base < b; base += 32) {
+            const int k = base + lane;
+            T t{};
+            const bool ok = k < b && test(k);
+            if (ok) t = term(k);
+            unsigned m = __ballot_sync(0xffffffffu, ok);
+            while (m) {  // the accepted candidates in order: lane order is candidate order
+                const int src = __ffs(m) - 1;
+                m &= m - 1u;
+                add(sum, shfl_from(t, src));
+            }
+        }
+    }
+
+    template <class T, class Test, class Term, class Add>
+    __device__ __forceinline__ static void window(const int* off, int dimx, int csx, int cex, int csy, int cey,
+                                                  Test&& test, Term&& term, Add&& add, T& sum) {
+        for (int cy = csy; cy <= cey; ++cy) {
+            const int row = cy * dimx;
+            span(off[row + csx], off[row + cex + 1], test, term, add, sum);
+        }
+    }
+};
+
+}  // namespace tss

@@ -114,16 +114,16 @@ cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
     }
     if ((e = mark(3, s)) != cudaSuccess) return e;
     // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
-    launch_k_density_high(batched, gather_grid[0], launch.threads[0], s, P, V);
+    launch_k_density_high(batched, launch.per_warp[0] != 0, gather_grid[0], launch.threads[0], s, P, V);
     if ((e = mark(4, s)) != cudaSuccess) return e;
-    launch_k_density_low(batched, gather_grid[1], launch.threads[1], s, P, V);
+    launch_k_density_low(batched, launch.per_warp[1] != 0, gather_grid[1], launch.threads[1], s, P, V);
     if ((e = mark(5, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
-    launch_k_force_low(batched, gather_grid[2], launch.threads[2], s, P, V);
+    launch_k_force_low(batched, launch.per_warp[2] != 0, gather_grid[2], launch.threads[2], s, P, V);
     if ((e = mark(6, s)) != cudaSuccess) return e;
     launch_k_split(batched, std::min(split_ntiles, 8 * sm_count()), kSplitThreads, s, P, V);
     if ((e = mark(7, s)) != cudaSuccess) return e;
-    launch_k_force_high(batched, gather_grid[3], launch.threads[3], s, P, V);
+    launch_k_force_high(batched, launch.per_warp[3] != 0, gather_grid[3], launch.threads[3], s, P, V);
     k_step_finish<<<1, 32, 0, s>>>(cnt);
     if ((e = mark(8, s)) != cudaSuccess) return e;
     return cudaGetLastError();
@@ -138,20 +138,22 @@ tss_status tss_solver::apply_launch(const tss_launch& l) {
         const int t = l.threads[g];
         if (t != 64 && t != 128 && t != 256) return fail(TSS_INVALID_ARG, "threads per block must be 64, 128 or 256");
         if (l.persistent[g] != 0 && l.persistent[g] != 1) return fail(TSS_INVALID_ARG, "persistent must be 0 or 1");
+        if (l.per_warp[g] != 0 && l.per_warp[g] != 1) return fail(TSS_INVALID_ARG, "per_warp must be 0 or 1");
     }
     const long long sms = sm_count();
     int grid[TSS_NUM_GATHERS];
     for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
         const int t = l.threads[g];
         const bool low = g == 1 || g == 2;
-        const long long cap = std::max(low ? nL : capH, 1);
+        const long long lanes = l.per_warp[g] ? 32 : 1;  // threads per particle
+        const long long cap = std::max(low ? nL : capH, 1) * lanes;
         const long long cover = (cap + t - 1) / t;
         if (l.persistent[g]) {
-            const int occ = gather_occupancy(g, batched, t);
+            const int occ = gather_occupancy(g, batched, l.per_warp[g] != 0, t);
             if (occ <= 0) return fail(TSS_CUDA_ERROR, "occupancy query of a gather kernel failed");
             grid[g] = static_cast<int>(sms * occ);
         } else if (low && low_full) {
-            grid[g] = static_cast<int>(cover);
+            grid[g] = static_cast<int>(std::min<long long>(cover, 0x7fffffffLL));
         } else {
             grid[g] = static_cast<int>(std::min(cover, sms * 4096 / t));
         }
@@ -167,6 +169,7 @@ tss_launch tss::default_launch() {
     for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
         l.threads[g] = 256;
         l.persistent[g] = 0;
+        l.per_warp[g] = 0;
     }
     return l;
 }
@@ -913,14 +916,18 @@ tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* b
     float best_ms[TSS_NUM_GATHERS];
     for (float& x : best_ms) x = 3.0e38f;
     int taken = 0;
-    // candidates in order: the default (256 threads, covering) first
-    const int cand_threads[6] = {256, 128, 64, 256, 128, 64};
-    const int cand_pers[6] = {0, 0, 0, 1, 1, 1};
-    for (int ci = 0; ci < 6 && st == TSS_OK; ++ci) {
+    // candidates in order: the default (256 threads, covering, a particle per
+    // thread) first; the last takes a particle per warp
+    constexpr int kCand = 7;
+    const int cand_threads[kCand] = {256, 128, 64, 256, 128, 64, 256};
+    const int cand_pers[kCand] = {0, 0, 0, 1, 1, 1, 0};
+    const int cand_warp[kCand] = {0, 0, 0, 0, 0, 0, 1};
+    for (int ci = 0; ci < kCand && st == TSS_OK; ++ci) {
         tss_launch c{};
         for (int g = 0; g < TSS_NUM_GATHERS; ++g) {
             c.threads[g] = cand_threads[ci];
             c.persistent[g] = cand_pers[ci];
+            c.per_warp[g] = cand_warp[ci];
         }
         if ((st = s->apply_launch(c)) != TSS_OK) break;
         // one untimed step captures the graph
@@ -940,6 +947,7 @@ tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* b
                 best_ms[g] = sum[g];
                 b.threads[g] = c.threads[g];
                 b.persistent[g] = c.persistent[g];
+                b.per_warp[g] = c.per_warp[g];
             }
     }
     if (st == TSS_OK) st = tss_solver_sync(s);  // a numeric or capacity error of the trial steps

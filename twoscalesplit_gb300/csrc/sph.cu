@@ -1,19 +1,24 @@
 // sph.cu -- density, force, split and relaxation kernels of the two-scale step.
 //
-// One thread per particle in (cell, id) order.  Because the arrays are sorted by
-// cell, the candidates of one row of the 3x3 (or wider cross-scale) cell window are
-// one contiguous span [off[row + cx0], off[row + cx1 + 1]), and consecutive threads
-// of a warp walk overlapping spans, so neighbour loads are coalesced and served from
-// L1.  Each thread sums its candidates in the reference's order (cells row by row,
-// particles in cell order), which keeps every FP32 sum identical to the reference's
-// for the same list order.
+// Particles are in (cell, id) order.  Because the arrays are sorted by cell, the
+// candidates of one row of the 3x3 (or wider cross-scale) cell window are one
+// contiguous span [off[row + cx0], off[row + cx1 + 1]).  Each particle's sums take
+// its candidates in the reference's order (cells row by row, particles in cell
+// order), which keeps every FP32 sum identical to the reference's for the same
+// list order.  The gathers walk a particle's window one of two ways (gather.cuh):
+// one particle per thread, consecutive threads walking overlapping spans so that
+// neighbour loads are shared through L1 (the throughput form), or one particle per
+// warp with the candidates spread over the lanes (for scenes too small to fill the
+// GPU); both give the same bits.
 //
 // Each kernel's per-particle work is an inlined function of the particle's Params:
 // the kernel's own constants for a single scene, the scene's table row for a
 // batch.  The row is read through a reference, so each field is loaded where it is
 // used: a copy of the whole row kept every field live in registers across the
-// neighbour loops, and the batched gathers spilled and ran 5 % slower.  A scene's cell windows index its grid at its cell base in the global
-// cell space, so one sort and one offset table serve all scenes of a batch.
+// neighbour loops, and the batched gathers spilled and ran 5 % slower.  A scene's
+// cell windows index its grid at its cell base in the global cell space, so one
+// sort and one offset table serve all scenes of a batch.
+#include "gather.cuh"
 #include "sph.cuh"
 
 namespace tss {
@@ -22,12 +27,26 @@ namespace {
 __device__ __forceinline__ int nthreads() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ int tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ float2 sub(float2 a, float2 b) { return sub2(a, b); }
+__device__ __forceinline__ void add_density(float& d, float t) { d += t; }
+
+// The particles of a gather, one per thread (G = PerThread) or one per warp
+// (G = PerWarp, every lane of the warp taking the same particle).
+template <class G, class F>
+__device__ __forceinline__ void for_each_particle(int n, F&& f) {
+    if constexpr (G::kWarp) {
+        const int nw = nthreads() >> 5;
+        for (int i = tid() >> 5; i < n; i += nw) f(i);
+    } else {
+        for (int i = tid(); i < n; i += nthreads()) f(i);
+    }
+}
 }  // namespace
 
 
 // ---------------------------------------------------------------------------
 // High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
 // ---------------------------------------------------------------------------
+template <class G>
 __device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
@@ -36,23 +55,19 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
     const float2 p = H.pos[i];
     const unsigned s = H.st[i];
     float d = 0.0f, dl = 0.0f;
+    float x = 0.0f;
+    const auto term = [&](int) { return pair_density(P, sqrtf(x)); };
     int csx, csy, cex, cey;
     grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
     grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-    {
-        Window w(offH, P.dimH[0], csx, cex, csy, cey);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
-                if (!lamHH(s, H.st[k])) return false;
-                x = sq(sub(p, H.pos[k]));
-                return x <= P.Tle_rh;
-            });
-            if (j < 0) break;
-            const float dist = sqrtf(x);
-            d += pair_density(P, dist);
-        }
-    }
+    G::window(
+        offH, P.dimH[0], csx, cex, csy, cey,
+        [&](int k) {
+            if (!lamHH(s, H.st[k])) return false;
+            x = sq(sub(p, H.pos[k]));
+            return x <= P.Tle_rh;
+        },
+        term, add_density, d);
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
     grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
     if (P.q1) {
@@ -63,151 +78,151 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
         const int nHs = offH[P.CHs] - baseH;
         for (int cy = csy; cy <= cey; ++cy) {
             const int row = cy * P.dimL[0];
-            const int b = offL[row + cex + 1];
-            for (int t = offL[row + csx]; t < b; ++t) {
-                const int tl = t - baseL;
-                float2 pj = make_float2(0.0f, 0.0f);
-                unsigned sj = 0;
-                if (tl < nHs) {
-                    pj = H.pos[baseH + tl];
-                    sj = H.st[baseH + tl];
-                } else {
-                    const int slot = 4 * P.sbL + tl;
-                    const int k = (tl < 4 * P.nLs && slot < P.slotsH) ? H.map[slot] : -1;
-                    if (k >= 0) {
-                        pj = H.pos[k];
-                        sj = H.st[k];
+            G::span(
+                offL[row + csx], offL[row + cex + 1],
+                [&](int t) {
+                    const int tl = t - baseL;
+                    float2 pj = make_float2(0.0f, 0.0f);
+                    unsigned sj = 0;
+                    if (tl < nHs) {
+                        pj = H.pos[baseH + tl];
+                        sj = H.st[baseH + tl];
+                    } else {
+                        const int slot = 4 * P.sbL + tl;
+                        const int k = (tl < 4 * P.nLs && slot < P.slotsH) ? H.map[slot] : -1;
+                        if (k >= 0) {
+                            pj = H.pos[k];
+                            sj = H.st[k];
+                        }
                     }
-                }
-                if (!lamHL(s, sj)) continue;
-                const float x = sq(sub(p, pj));
-                if (x <= P.Tle_rh) {
-                    const float dist = sqrtf(x);
-                    d += pair_density(P, dist);
-                }
-            }
+                    if (!lamHL(s, sj)) return false;
+                    x = sq(sub(p, pj));
+                    return x <= P.Tle_rh;
+                },
+                term, add_density, d);
         }
     } else {
-        Window w(offL, P.dimL[0], csx, cex, csy, cey);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
+        G::window(
+            offL, P.dimL[0], csx, cex, csy, cey,
+            [&](int k) {
                 if (!lamHL(s, L.st[k])) return false;
                 x = sq(sub(p, L.pos[k]));
                 return x <= P.Tle_rh;
-            });
-            if (j < 0) break;
-            const float dist = sqrtf(x);
-            dl += pair_density(P, dist);
-        }
+            },
+            term, add_density, dl);
     }
     d *= P.mH;
     dl *= P.mL;
     d += dl;
     const float pr = tait(d, P);
-    H.dens[i] = d;
-    H.pres[i] = pr;
-    H.q[i] = pr / (d * d);
-    if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    if (G::leader()) {
+        H.dens[i] = d;
+        H.pres[i] = pr;
+        H.q[i] = pr / (d * d);
+        if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    }
 }
 
-template <bool B>
+template <bool B, class G>
 __global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
-    const int n = V.cnt->cur[1];
-    for (int i = tid(); i < n; i += nthreads()) {
+    for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];
-            density_high_one(P, V, i);
+            density_high_one<G>(P, V, i);
         } else {
-            density_high_one(P0, V, i);
+            density_high_one<G>(P0, V, i);
         }
-    }
+    });
 }
 
 // ---------------------------------------------------------------------------
 // Low-res density + Tait, computeParticleDensityPressure (WCSPHSolver.cu:1342-1424)
 // ---------------------------------------------------------------------------
+template <class G>
 __device__ __forceinline__ void density_low_one(const Params& P, const StepView& V, int i, bool cross) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     const float2 p = L.pos[i];
     const unsigned s = L.st[i];
     float d = 0.0f, dh = 0.0f;
+    float x = 0.0f;
+    const auto term = [&](int) { return pair_density(P, sqrtf(x)); };
     int csx, csy, cex, cey;
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
     grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-    {
-        Window w(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
-                x = sq(sub(p, L.pos[k]));
-                return x <= P.Tle_r;
-            });
-            if (j < 0) break;
-            const float dist = sqrtf(x);
-            d += pair_density(P, dist);
-        }
-    }
+    G::window(
+        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
+        [&](int k) {
+            x = sq(sub(p, L.pos[k]));
+            return x <= P.Tle_r;
+        },
+        term, add_density, d);
     if (cross) {  // only state-0 high-res particles can contribute (lambda_LH)
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        Window w(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
+        G::window(
+            H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
+            [&](int k) {
                 if (!lamLH(s, H.st[k])) return false;
                 x = sq(sub(p, H.pos[k]));
                 return x <= P.Tle_r;
-            });
-            if (j < 0) break;
-            const float dist = sqrtf(x);
-            dh += pair_density(P, dist);
-        }
+            },
+            term, add_density, dh);
     }
     d *= P.mL;
     dh *= P.mH;
     const float rho = d + dh;
     const float pr = tait(rho, P);
-    L.dens[i] = rho;
-    L.pres[i] = pr;
-    L.q[i] = pr / (rho * rho);
-    if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    if (G::leader()) {
+        L.dens[i] = rho;
+        L.pres[i] = pr;
+        L.q[i] = pr / (rho * rho);
+        if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
+    }
 }
 
-template <bool B>
+template <bool B, class G>
 __global__ void __launch_bounds__(256) k_density_low(Params P0, StepView V) {
-    const int n = V.cnt->cur[0];
     const bool cross = V.cnt->h_state0 != 0;
-    for (int i = tid(); i < n; i += nthreads()) {
+    for_each_particle<G>(V.cnt->cur[0], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scL[i]];
-            density_low_one(P, V, i, cross);
+            density_low_one<G>(P, V, i, cross);
         } else {
-            density_low_one(P0, V, i, cross);
+            density_low_one<G>(P0, V, i, cross);
         }
-    }
+    });
 }
 
 // Wall term of a force sum (updateAccCell 562-579 / updateAccCellComplementHigh
 // 867-884): every wall particle of the window's cells, in cell order.  Pairs with
 // sqrtf(x) > rad have q >= 2 and add exactly zero, so they are skipped.
+template <class G>
 __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, float2 p, int csx, int cex, int csy,
                                            int cey, float rad, float Tle, float cB) {
     float2 accB = make_float2(0.f, 0.f);
     const int* woff = V.woff + P.cbL;
     const float2* wpos = V.wpos + P.wb;
+    float2 pik = make_float2(0.f, 0.f);
+    float x = 0.0f;
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimL[0];
-        const int wb = woff[row + cex + 1];
-        for (int k = woff[row + csx]; k < wb; ++k) {
-            const float2 pik = sub(p, wpos[k]);
-            const float x = sq(pik);
-            if (x > Tle) continue;  // NaN passes: the reference's 0 * NaN offset propagates it
-            const float gm = wall_weight(sqrtf(x), rad, P.cs);
-            accB.x += cB * gm * pik.x;
-            accB.y += cB * gm * pik.y;
-        }
+        G::span(
+            woff[row + csx], woff[row + cex + 1],
+            [&](int k) {
+                pik = sub(p, wpos[k]);
+                x = sq(pik);
+                return !(x > Tle);  // NaN passes: the reference's 0 * NaN offset propagates it
+            },
+            [&](int) {
+                const float gm = wall_weight(sqrtf(x), rad, P.cs);
+                return make_float2(cB * gm * pik.x, cB * gm * pik.y);
+            },
+            [](float2& a, float2 t) {
+                a.x += t.x;
+                a.y += t.y;
+            },
+            accB);
     }
     return accB;
 }
@@ -219,48 +234,46 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
 // accumulators, so they are taken in two passes over the window.  The new position
 // also gives the entry's key for the next step's grid.  Returns the split flag.
 // ---------------------------------------------------------------------------
+template <class G>
 __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V, int i, bool cross) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     float2 p = L.pos[i], v = L.vel[i];
     const unsigned s = L.st[i];
     const float dens = L.dens[i], qi = L.q[i];
-    float2 acc = make_float2(0.f, 0.f), accH = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
+    PairTerms fl{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // (acc, accT)
+    float2 pij = make_float2(0.f, 0.f);
+    float x = 0.0f;
     int csx, csy, cex, cey;
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
     grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-    {
-        Window w(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey);
-        float2 pij = make_float2(0.f, 0.f);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
-                pij = sub(p, L.pos[k]);
-                x = sq(pij);
-                return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
-            });
-            if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r, acc, accT);
-        }
-    }
-    const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
+    G::window(
+        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
+        [&](int k) {
+            pij = sub(p, L.pos[k]);
+            x = sq(pij);
+            return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
+        },
+        [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r); },
+        add_terms, fl);
+    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
+    PairTerms fh{make_float2(0.f, 0.f), fl.t};  // (accH, accT): the sigma sum continues
     if (cross) {
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
         grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-        Window w(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey);
-        float2 pij = make_float2(0.f, 0.f);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
+        G::window(
+            H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
+            [&](int k) {
                 if (!lamLH(s, H.st[k])) return false;
                 pij = sub(p, H.pos[k]);
                 x = sq(pij);
                 return x != 0.0f && x <= P.Tlt_r;
-            });
-            if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx, accH, accT);
-        }
+            },
+            [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx); },
+            add_terms, fh);
     }
+    float2 acc = fl.a, accH = fh.a;
+    const float2 accT = fh.t;
     acc.x *= -P.mL;
     acc.y *= -P.mL;
     accH.x *= -P.mH;
@@ -272,17 +285,10 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     acc.x += accB.x;
     acc.y += accB.y;
     acc.y -= P.g;
-    L.acc[i] = acc;
-    if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
     v.x += P.dt * acc.x;
     v.y += P.dt * acc.y;
     p.x += P.dt * v.x;
     p.y += P.dt * v.y;
-    L.npos[i] = p;
-    L.nvel[i] = v;
-    L.nid[i] = L.id[i];
-    grid_key(L.gcount, L.gkey, L.grank, L.gtile, i,
-             P.cbL + cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
     // split test on the predicted position (computeParticleAcceleration 1810-1835)
     // against the ROI of this step; with TSS_FLAG_MERGE a split parent outside it
     // merges back
@@ -298,38 +304,54 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     } else if (P.merge && s == 1u && !in_roi) {
         ns = 0;
     }
-    L.nst[i] = ns;
-    V.split_flag[i] = flag ? 1 : 0;
-    if (L.ndens) {
-        L.ndens[i] = dens;
-        L.npres[i] = L.pres[i];
+    if (G::leader()) {
+        L.acc[i] = acc;
+        if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+        L.npos[i] = p;
+        L.nvel[i] = v;
+        L.nid[i] = L.id[i];
+        grid_key(L.gcount, L.gkey, L.grank, L.gtile, i,
+                 P.cbL + cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
+        L.nst[i] = ns;
+        V.split_flag[i] = flag ? 1 : 0;
+        if (L.ndens) {
+            L.ndens[i] = dens;
+            L.npres[i] = L.pres[i];
+        }
     }
     return flag;
 }
 
-// Warp-uniform loop: every lane makes the same number of trips (lanes past n are
-// inactive) so the ballot that feeds the split compaction sees whole warps; a
-// warp's 32 particles lie in one compaction tile (kSplitTile % 32 == 0).
+// One particle per thread: a warp-uniform loop (every lane makes the same number of
+// trips, lanes past n inactive) so the ballot that feeds the split compaction sees
+// whole warps; a warp's 32 particles lie in one compaction tile (kSplitTile % 32 ==
+// 0).  One particle per warp: the leader counts its particle's split.
 // Register budgets measured per form: the single-scene form at 48 registers (five
 // blocks per SM), the batched form at 40 (six).
-template <bool B>
+template <bool B, class G>
 __global__ void __launch_bounds__(256, B ? 6 : 5) k_force_low(Params P0, StepView V) {
     const int n = V.cnt->cur[0];
     const bool cross = V.cnt->h_state0 != 0;
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        bool flag = false;
-        if (i < n) {
-            if constexpr (B) {
-                const Params& P = V.table[V.scL[i]];
-                flag = force_low_one(P, V, i, cross);
-            } else {
-                flag = force_low_one(P0, V, i, cross);
-            }
+    const auto one = [&](int i) {
+        if constexpr (B) {
+            const Params& P = V.table[V.scL[i]];
+            return force_low_one<G>(P, V, i, cross);
+        } else {
+            return force_low_one<G>(P0, V, i, cross);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, flag);
-        if (lane == 0 && m) atomicAdd(&V.split_tile[(base + (threadIdx.x & ~31)) / kSplitTile], __popc(m));
+    };
+    if constexpr (G::kWarp) {
+        for_each_particle<G>(n, [&](int i) {
+            if (one(i) && G::leader()) atomicAdd(&V.split_tile[i / kSplitTile], 1u);
+        });
+    } else {
+        const int lane = threadIdx.x & 31;
+        for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+            const int i = base + threadIdx.x;
+            const bool flag = i < n && one(i);
+            const unsigned m = __ballot_sync(0xffffffffu, flag);
+            if (lane == 0 && m) atomicAdd(&V.split_tile[(base + (threadIdx.x & ~31)) / kSplitTile], __popc(m));
+        }
     }
 }
 
@@ -457,50 +479,46 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) 
 // Reads see the pre-step state (the reference integrates in place, a data race);
 // low-res states are read after this step's split marks, as in the reference.
 // ---------------------------------------------------------------------------
+template <class G>
 __device__ __forceinline__ void force_high_one(const Params& P, const StepView& V, int i) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     float2 p = H.pos[i], v = H.vel[i];
     const unsigned s = H.st[i];
     const float dens = H.dens[i], qi = H.q[i];
-    float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accT = make_float2(0.f, 0.f);
+    PairTerms fh{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // (acc, accT)
+    float2 pij = make_float2(0.f, 0.f);
+    float x = 0.0f;
     int csx, csy, cex, cey;
     grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
     grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
-    {
-        Window w(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey);
-        float2 pij = make_float2(0.f, 0.f);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
-                if (!lamHH(s, H.st[k])) return false;
-                pij = sub(p, H.pos[k]);
-                x = sq(pij);
-                return x != 0.0f && x <= P.Tlt_rh;
-            });
-            if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh, acc, accT);
-        }
-    }
+    G::window(
+        H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
+        [&](int k) {
+            if (!lamHH(s, H.st[k])) return false;
+            pij = sub(p, H.pos[k]);
+            x = sq(pij);
+            return x != 0.0f && x <= P.Tlt_rh;
+        },
+        [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh); },
+        add_terms, fh);
     grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
     grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
-    {
-        Window w(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey);
-        float2 pij = make_float2(0.f, 0.f);
-        float x = 0.0f;
-        for (;;) {
-            const int j = w.next([&](int k) {
-                const unsigned sj = L.nst[k];  // low-res states after this step's split marks
-                if (!(lamHL(s, sj) && notDeleted(sj))) return false;
-                pij = sub(p, L.pos[k]);
-                x = sq(pij);
-                return x != 0.0f && x <= P.Tlt_r;
-            });
-            if (j < 0) break;
-            pair_force(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx, accL, accT);
-        }
-    }
-    const float2 accB = wall_sum(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
+    PairTerms fl{make_float2(0.f, 0.f), fh.t};  // (accL, accT): the sigma sum continues
+    G::window(
+        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
+        [&](int k) {
+            const unsigned sj = L.nst[k];  // low-res states after this step's split marks
+            if (!(lamHL(s, sj) && notDeleted(sj))) return false;
+            pij = sub(p, L.pos[k]);
+            x = sq(pij);
+            return x != 0.0f && x <= P.Tlt_r;
+        },
+        [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx); },
+        add_terms, fl);
+    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
+    float2 acc = fh.a, accL = fl.a;
+    const float2 accT = fl.t;
     acc.x *= -P.mH;
     acc.y *= -P.mH;
     accL.x *= -P.mL;
@@ -512,8 +530,6 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     acc.x += accB.x;
     acc.y += accB.y;
     acc.y -= P.g;
-    H.acc[i] = acc;
-    if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
     v.x += P.dt * acc.x;
     v.y += P.dt * acc.y;
     p.x += P.dt * v.x;
@@ -540,6 +556,9 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
             }
         }
     }
+    if (!G::leader()) return;
+    H.acc[i] = acc;
+    if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
     H.npos[i] = p;
     H.nvel[i] = v;
     H.nst[i] = static_cast<uint8_t>(drop ? 2u : s);
@@ -558,19 +577,18 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
 }
 
 // The batched form reads each particle's parameters from the scene table; at 40
-// registers it spills ~300 bytes, at 48 (five blocks per SM) a third of that, which
+// registers it spilled ~300 bytes, at 48 (five blocks per SM) a third of that, which
 // measured 5 % faster on the mixed batch (the single-scene form keeps six blocks).
-template <bool B>
+template <bool B, class G>
 __global__ void __launch_bounds__(256, B ? 5 : 6) k_force_high(Params P0, StepView V) {
-    const int n = V.cnt->cur[1];
-    for (int i = tid(); i < n; i += nthreads()) {
+    for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];
-            force_high_one(P, V, i);
+            force_high_one<G>(P, V, i);
         } else {
-            force_high_one(P0, V, i);
+            force_high_one<G>(P0, V, i);
         }
-    }
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -743,7 +761,30 @@ __global__ void k_step_finish(Counters* c) {
     }
 }
 
-// Host-side launchers (the templates stay in this translation unit).
+// Host-side launchers (the templates stay in this translation unit).  A gather's
+// launcher selects the batched form (B) and the walk (one particle per thread or
+// per warp).
+#define TSS_GATHER_LAUNCHER(NAME)                                                                   \
+    void launch_##NAME(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P, \
+                       const StepView& V) {                                                          \
+        if (batched) {                                                                               \
+            if (warp)                                                                                \
+                NAME<true, PerWarp><<<blocks, threads, 0, s>>>(P, V);                                \
+            else                                                                                     \
+                NAME<true, PerThread><<<blocks, threads, 0, s>>>(P, V);                              \
+        } else {                                                                                     \
+            if (warp)                                                                                \
+                NAME<false, PerWarp><<<blocks, threads, 0, s>>>(P, V);                               \
+            else                                                                                     \
+                NAME<false, PerThread><<<blocks, threads, 0, s>>>(P, V);                             \
+        }                                                                                            \
+    }
+TSS_GATHER_LAUNCHER(k_density_high)
+TSS_GATHER_LAUNCHER(k_density_low)
+TSS_GATHER_LAUNCHER(k_force_low)
+TSS_GATHER_LAUNCHER(k_force_high)
+#undef TSS_GATHER_LAUNCHER
+
 #define TSS_LAUNCHER(NAME)                                                                        \
     void launch_##NAME(bool batched, int blocks, int threads, cudaStream_t s, const Params& P,   \
                        const StepView& V) {                                                       \
@@ -752,41 +793,41 @@ __global__ void k_step_finish(Counters* c) {
         else                                                                                      \
             NAME<false><<<blocks, threads, 0, s>>>(P, V);                                         \
     }
-TSS_LAUNCHER(k_density_high)
-TSS_LAUNCHER(k_density_low)
-TSS_LAUNCHER(k_force_low)
 TSS_LAUNCHER(k_split)
-TSS_LAUNCHER(k_force_high)
 TSS_LAUNCHER(k_relax_density)
 TSS_LAUNCHER(k_relax_force)
 #undef TSS_LAUNCHER
 
-// Resident blocks per SM of gather g (0 high-res density, 1 low-res density,
-// 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error.
-int gather_occupancy(int g, bool batched, int threads) {
+namespace {
+template <class K>
+int occupancy(K kernel, int threads) {
     int n = 0;
-    cudaError_t e = cudaErrorInvalidValue;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) == cudaSuccess ? n : 0;
+}
+
+template <bool B, class G>
+int gather_occupancy_of(int g, int threads) {
     switch (g) {
         case 0:
-            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_high<true>, threads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_high<false>, threads, 0);
-            break;
+            return occupancy(k_density_high<B, G>, threads);
         case 1:
-            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_low<true>, threads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_density_low<false>, threads, 0);
-            break;
+            return occupancy(k_density_low<B, G>, threads);
         case 2:
-            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_low<true>, threads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_low<false>, threads, 0);
-            break;
+            return occupancy(k_force_low<B, G>, threads);
         case 3:
-            e = batched ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_high<true>, threads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force_high<false>, threads, 0);
-            break;
+            return occupancy(k_force_high<B, G>, threads);
         default:
-            break;
+            return 0;
     }
-    return e == cudaSuccess ? n : 0;
+}
+}  // namespace
+
+// Resident blocks per SM of gather g (0 high-res density, 1 low-res density,
+// 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error.
+int gather_occupancy(int g, bool batched, bool warp, int threads) {
+    if (batched)
+        return warp ? gather_occupancy_of<true, PerWarp>(g, threads) : gather_occupancy_of<true, PerThread>(g, threads);
+    return warp ? gather_occupancy_of<false, PerWarp>(g, threads) : gather_occupancy_of<false, PerThread>(g, threads);
 }
 
 }  // namespace tss

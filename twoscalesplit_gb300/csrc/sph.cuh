@@ -55,27 +55,29 @@ constexpr int kSplitTile = kSplitThreads * kSplitItems;
 
 // B = false: one scene, parameters P0 (kernel constants).  B = true: a batch of
 // scenes; each particle's parameters are V.table[scene of the particle], and each
-// scene's grids sit at its cell bases in one global cell space.
-template <bool B> __global__ void k_density_high(Params P0, StepView V);
-template <bool B> __global__ void k_density_low(Params P0, StepView V);
-template <bool B> __global__ void k_force_low(Params P0, StepView V);
+// scene's grids sit at its cell bases in one global cell space.  The gathers
+// (densities, forces) are further templated on how a particle's window is walked
+// (gather.cuh) and launched through the launchers below.
 template <bool B> __global__ void k_split(Params P0, StepView V);
-template <bool B> __global__ void k_force_high(Params P0, StepView V);
 template <bool B> __global__ void k_relax_density(Params P0, StepView V);
 template <bool B> __global__ void k_relax_force(Params P0, StepView V);
 __global__ void k_relax_apply(Params P0, StepView V);
 __global__ void k_step_finish(Counters* c);
 
-// host launchers of the templates above (batched selects B)
-void launch_k_density_high(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
-void launch_k_density_low(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
-void launch_k_force_low(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
+// host launchers (batched selects B; warp: one particle per warp instead of per thread)
+void launch_k_density_high(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
+                           const StepView& V);
+void launch_k_density_low(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
+                          const StepView& V);
+void launch_k_force_low(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
+                        const StepView& V);
+void launch_k_force_high(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
+                         const StepView& V);
 void launch_k_split(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
-void launch_k_force_high(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 void launch_k_relax_density(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 void launch_k_relax_force(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 // resident blocks per SM of gather g (0 high-res density, 1 low-res density,
 // 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error
-int gather_occupancy(int g, bool batched, int threads);
+int gather_occupancy(int g, bool batched, bool warp, int threads);
 
 }  // namespace tss

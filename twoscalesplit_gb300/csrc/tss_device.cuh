@@ -180,12 +180,19 @@ __device__ __forceinline__ bool lamHH(unsigned si, unsigned sj) { return !((si &
 __device__ __forceinline__ bool lamHL(unsigned si, unsigned sj) { return !((si & 1u) && (sj & 1u)); }        // {1,1,1,0}
 __device__ __forceinline__ bool notDeleted(unsigned s) { return s < 2u; }                       // {1,1,0}
 
+// The two terms of a force pair: a for the pressure/viscosity sum, t for the
+// sigma sum.
+struct PairTerms {
+    float2 a, t;
+};
+
 // One pair of a force sum: the body of updateAccCell / updateAccCellComplement /
 // updateAccCellHigh / updateAccCellComplementHigh (WCSPHSolver.cu:521-558 etc.).
 // qi, qj are p/rho^2 of the two particles (the reference's pre/dens2, prej/densj2).
-// Both scales' kernels are evaluated as float2 pairs (kern2).
-__device__ __forceinline__ void pair_force(const Params& P, float2 pij, float dist, float2 vij, float qi, float qj,
-                                           float densi, float densj, float h, float2& acc, float2& accT) {
+// Both scales' kernels are evaluated as float2 pairs (kern2).  Each sum adds one
+// term per pair, so a pair's terms may be evaluated apart from the sums.
+__device__ __forceinline__ PairTerms pair_terms(const Params& P, float2 pij, float dist, float2 vij, float qi,
+                                                float qj, float densi, float densj, float h) {
     const float2 vp = mul2(vij, pij);
     const float dvp = vp.x + vp.y;
     const float visc = dvp / (dist * dist + 0.01f * h * h) * 2.0f * h * P.alpha * P.cs / (densi + densj);
@@ -198,8 +205,13 @@ __device__ __forceinline__ void pair_force(const Params& P, float2 pij, float di
     const float ww = w.x + w.y;
     const float2 half = make_float2(0.5f, 0.5f);  // x / 2 == x * 0.5 exactly
     const float2 g = make_float2(gI.x + gJ.x, gI.y + gJ.y);  // products: added in scalar (see add2)
-    acc = add2(acc, mul2(mul2(make_float2(coeff, coeff), g), half));
-    accT = add2(accT, mul2(mul2(pij, make_float2(ww, ww)), half));
+    return PairTerms{mul2(mul2(make_float2(coeff, coeff), g), half), mul2(mul2(pij, make_float2(ww, ww)), half)};
+}
+
+// adds a pair's terms to the force sums (acc, accT) = (s.a, s.t)
+__device__ __forceinline__ void add_terms(PairTerms& s, const PairTerms& t) {
+    s.a = add2(s.a, t.a);
+    s.t = add2(s.t, t.t);
 }
 
 // The density term of a pair at distance d: the symmetrised kernel

@@ -584,6 +584,16 @@ def run_serve(args):
     numeric_served = sorted(k for k, st in enumerate(stats) if st["status"] == _abi.TSS_NUMERIC)
     numeric_plain = []
     # 3. the plain solver, one request at a time, each timed (create + steps + download)
+    #    with the launch shape tuned for its size class; the classes are tuned first,
+    #    on scratch solvers, so that no request takes trial steps
+    if not args.no_plain and not args.no_autotune:
+        from twoscalesplit_gb300 import tuning
+        seen = set()
+        for sc, _, _ in trace:
+            cls = tuning.workload_class("single", sc.n_low)
+            if cls not in seen:
+                seen.add(cls)
+                tuned_shape(Solver.from_scene(sc), "single", sc.n_low, args)
     service = np.zeros(len(trace))
     exact = 0
     plain_steps_ms = 0.0
@@ -591,6 +601,8 @@ def run_serve(args):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         sol = Solver.from_scene(sc)
+        if not args.no_autotune:
+            tuned_shape(sol, "single", sc.n_low, args)  # from the cache: no steps
         sol.step(h)
         lo, hi = sol.download(0), sol.download(1)
         service[k] = time.perf_counter() - t0

@@ -132,3 +132,20 @@ def test_read_positions_equals_download_and_refuses_pageable_memory():
     assert np.array_equal(short.numpy(), low.numpy()[:3])
     with pytest.raises(TssError):
         sol.read_positions(torch.zeros((sc.n_low, 2), dtype=torch.float32), high, counts, stream=stream)
+
+
+@pytest.mark.parametrize("relax", [0, 4])
+def test_one_particle_per_warp_through_merges_and_the_guard(relax):
+    """The moving region of interest with merging, the tether guard and (without
+    Q1) the low-res cross term, one particle per warp against one per thread."""
+    sc = scenes.adaptive_dam_break(40, 80, 0.01, roi_velocity=(20.0, 5.0), roi_start=(0.0, 0.05), steps=120,
+                                   relax_iters=relax)
+    ref = Solver.from_scene(sc)
+    sol = Solver.from_scene(sc)
+    sol.set_launch(_shape(128, False, True))
+    ref.step(120)
+    sol.step(120)
+    c = sol.counts()
+    assert c["total_split"] > 0 and c["total_removed"] > 0
+    assert c == ref.counts()
+    _assert_same(_state(ref), _state(sol))

@@ -142,6 +142,16 @@ public:
     }
     tss_solver* handle() { return mS; }
 
+    // Launch-shape autotuner (tss_solver_autotune; not in the reference): times the
+    // candidate shapes on this solver's own steps, which advance its state, and
+    // installs the fastest per gather.
+    tss_launch Autotune(int stepsPerTrial = 3) {
+        if (!mS) Bind();
+        tss_launch l;
+        throw_on(tss_solver_autotune(mS, stepsPerTrial, &l, nullptr), mS);
+        return l;
+    }
+
     tss_buffers buffers() {
         tss_buffers b;
         throw_on(tss_solver_device_buffers(mS, &b), mS);

@@ -469,7 +469,7 @@ def run_batch(args):
     lockstep by one batch (one grid build and one launch of each kernel per step),
     against the same scenes advanced one at a time by the plain solver."""
     import torch
-    from twoscalesplit_gb300 import build, scenes
+    from twoscalesplit_gb300 import _abi, build, scenes
     from twoscalesplit_gb300.solver import Batch, Solver
     build.build()
     dev = torch.device("cuda", 0)
@@ -503,6 +503,16 @@ def run_batch(args):
     batch_ms = sum(x.elapsed_time(y) for x, y in evs)
     c = b.counts()
     parts_end = c["n_low"] + c["n_high"]
+    # where a step's time goes once the high-res lists have filled: stage times
+    # (profiling graph) of 10 more steps from the final state, untimed above
+    b.profile(True)
+    st_sum = {k: 0.0 for k in _abi.STAGE_NAMES}
+    for _ in range(10):
+        flush.zero_()
+        b.step(1, stream=sh)
+        for name, v in b.stage_times().items():
+            st_sum[name] += v
+    b.profile(False)
     del b
     # the plain solver, one scene at a time, same steps
     plain_ms = 0.0
@@ -530,7 +540,8 @@ def run_batch(args):
             "particle_steps_per_s": n_low * K / (batch_ms / 1e3),
             "plain_one_at_a_time": {"scene_steps_per_s": len(scs) * K / (plain_ms / 1e3),
                                     "sampled_scenes": n_plain, "ms_per_lockstep": plain_ms / K},
-            "speedup_vs_plain": plain_ms / batch_ms, "clocks": clk, "n_particles_end": parts_end}
+            "speedup_vs_plain": plain_ms / batch_ms, "clocks": clk, "n_particles_end": parts_end,
+            "stage_ms_end": {k: round(v / 10, 4) for k, v in st_sum.items()}}
     print(json.dumps(line), flush=True)
 
 

@@ -73,27 +73,37 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
     if (P.q1) {
         // The reference reads the HIGH sorted list at LOW-grid ranges of its own
         // scene; past the scene's n_high that list still holds its initial identity
-        // (slot t at position t).
+        // (slot t at position t).  A row's range [a, b) of low-list positions t
+        // (t - baseL >= 0: offsets only grow) is taken in two runs, in order: the
+        // positions below baseL + n_high, which are the high-list entries
+        // t - baseL + baseH, and the rest, through the slot map.
         const int baseL = offL[0], baseH = offH[0];
         const int nHs = offH[P.CHs] - baseH;
+        const int tH = baseL + nHs;   // first position past the scene's high-res list
+        const int dH = baseH - baseL;  // low-list position -> high-list entry
         for (int cy = csy; cy <= cey; ++cy) {
             const int row = cy * P.dimL[0];
+            const int a = offL[row + csx], b = offL[row + cex + 1];
+            const int m = min(b, max(a, tH));
             G::span(
-                offL[row + csx], offL[row + cex + 1],
+                a + dH, m + dH,
+                [&](int k) {
+                    if (!lamHL(s, H.st[k])) return false;
+                    x = sq(sub(p, H.pos[k]));
+                    return x <= P.Tle_rh;
+                },
+                term, add_density, d);
+            G::span(
+                m, b,
                 [&](int t) {
                     const int tl = t - baseL;
+                    const int slot = 4 * P.sbL + tl;
+                    const int k = (tl < 4 * P.nLs && slot < P.slotsH) ? H.map[slot] : -1;
                     float2 pj = make_float2(0.0f, 0.0f);
                     unsigned sj = 0;
-                    if (tl < nHs) {
-                        pj = H.pos[baseH + tl];
-                        sj = H.st[baseH + tl];
-                    } else {
-                        const int slot = 4 * P.sbL + tl;
-                        const int k = (tl < 4 * P.nLs && slot < P.slotsH) ? H.map[slot] : -1;
-                        if (k >= 0) {
-                            pj = H.pos[k];
-                            sj = H.st[k];
-                        }
+                    if (k >= 0) {
+                        pj = H.pos[k];
+                        sj = H.st[k];
                     }
                     if (!lamHL(s, sj)) return false;
                     x = sq(sub(p, pj));

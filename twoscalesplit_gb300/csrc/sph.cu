@@ -586,11 +586,14 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     }
 }
 
-// The batched form reads each particle's parameters from the scene table; at 40
-// registers it spilled ~300 bytes, at 48 (five blocks per SM) a third of that, which
-// measured 5 % faster on the mixed batch (the single-scene form keeps six blocks).
+// Register budgets measured per form.  The batched form reads each particle's
+// parameters from the scene table: at 40 registers it spilled ~300 bytes, at 48 a
+// third of that, at 64 (four blocks per SM) nothing -- as fast as 48 on a batch of
+// 512 mixed scenes and 15 % faster on a batch of one 162k-particle scene.  The
+// single-scene form at 48 registers (five blocks) spills 64 bytes instead of 120
+// at 40 and measured 3-4 % faster.
 template <bool B, class G>
-__global__ void __launch_bounds__(256, B ? 5 : 6) k_force_high(Params P0, StepView V) {
+__global__ void __launch_bounds__(256, B ? 4 : 5) k_force_high(Params P0, StepView V) {
     for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];

@@ -66,6 +66,7 @@ typedef struct tss_config {
     int   dims_high[2];       /* ceil((end - origin) / r_high)  (WCSPHSolver.cu:2328-2331) */
     float r_low;              /* EffectiveRadius: support radius of the low-res scale      */
     float r_high;             /* EffectiveRadiusHigh                                        */
+                              /* both in [2^-40, 2^40], else TSS_INVALID_ARG at creation    */
     float rest_density;
     float tait_b;             /* Tait coefficient B in p = B((rho/rho0)^7 - 1)              */
     float speed_sound;

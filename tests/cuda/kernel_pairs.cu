@@ -48,6 +48,8 @@ int main(int argc, char** argv) {
     P.CL = static_cast<float>(10.0 / (7.0 * pi * P.r * P.r));
     P.CH = static_cast<float>(10.0 / (7.0 * pi * P.rh * P.rh));
     P.GL = static_cast<float>(-30.0 / (7.0 * pi * P.r * P.r * P.r));
+    recip_split(P.r, P.inv_hi.x, P.inv_lo.x);
+    recip_split(P.rh, P.inv_hi.y, P.inv_lo.y);
     P.GH = static_cast<float>(-30.0 / (7.0 * pi * P.rh * P.rh * P.rh));
     std::mt19937 rng(1);
     std::uniform_real_distribution<float> u(0.0f, 1.0f);

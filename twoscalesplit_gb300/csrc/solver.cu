@@ -281,9 +281,14 @@ void launch_keys_batched(const float2* pos, const int32_t* id, const int* n_ptr,
                                                                            page_shift, shift, high, g);
 }
 
+// Support radii in [2^-40, 2^40] (about 1e-12 to 1e12): the range in which the
+// pair kernels' division by a radius (div_const) is exact.  The reference's own
+// gradient coefficient -120/(14 pi r^3) overflows FP32 below about 1e-13.
+bool in_radius_range(float r) { return r >= 0x1p-40f && r <= 0x1p40f; }
+
 bool valid_cfg(const tss_config* cfg) {
     if (!cfg || !finite_cfg(cfg) || cfg->dims_low[0] <= 0 || cfg->dims_low[1] <= 0 || cfg->dims_high[0] <= 0 ||
-        cfg->dims_high[1] <= 0 || !(cfg->r_low > 0) || !(cfg->r_high > 0) || cfg->relax_iters < 0 ||
+        cfg->dims_high[1] <= 0 || !in_radius_range(cfg->r_low) || !in_radius_range(cfg->r_high) || cfg->relax_iters < 0 ||
         cfg->relax_iters > 64 || !(cfg->relax_dt_div > 0))
         return false;
     return static_cast<long long>(cfg->dims_low[0]) * cfg->dims_low[1] < (1LL << 31) - 2 &&
@@ -333,6 +338,8 @@ Params make_params(const SceneIn& sc) {
     P.Tlt_r = sq_cutoff(P.r, false);
     P.Tle_rh = sq_cutoff(P.rh, true);
     P.Tlt_rh = sq_cutoff(P.rh, false);
+    recip_split(P.r, P.inv_hi.x, P.inv_lo.x);
+    recip_split(P.rh, P.inv_hi.y, P.inv_lo.y);
     P.nLs = sc.n_low;
     P.CHs = cfg->dims_high[0] * cfg->dims_high[1];
     return P;

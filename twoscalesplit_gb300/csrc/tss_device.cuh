@@ -4,6 +4,7 @@
 // --fmad=false and IEEE division/square root, so a kernel's result is the
 // reference's result for the same summation order, bit for bit.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -43,7 +44,60 @@ struct Params {
     // x <= Tlt_s  <=>  sqrtf(x) < r_s, for x = dx*dx + dy*dy (IEEE sqrt is monotone
     // and correctly rounded, so these are the largest floats with that property)
     float Tle_r, Tlt_r, Tle_rh, Tlt_rh;
+    // reciprocal splits of (r, rh) for div_const: hi = RN(1/r_s), lo = RN(1/r_s - hi)
+    float2 inv_hi, inv_lo;
 };
+
+// Division by a per-scene constant b (the smoothing lengths), correctly rounded:
+// the IEEE quotient RN(a/b) from the reciprocal split yh = RN(1/b), yl ~ 1/b - yh
+// (recip_split), in three fused multiply-adds and a multiply:
+//   q0 = RN(a*yh + RN(a*yl))   a*(yh + yl) is a/b to ~2^-47, so q0 is within one ulp
+//   r  = a - q0*b              exact: the remainder of a quotient within one ulp
+//   q  = RN(q0 + r*yh)         = RN(a/b) by Markstein's theorem (yh within half an
+//                              ulp of 1/b, q0 within one ulp of a/b)
+// (P. W. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Develop. 34(1):111-119, 1990; J.-M. Muller
+// et al., Handbook of Floating-Point Arithmetic, chapter on division with an FMA.)
+// The theorem needs every step in the normal range.  The callers divide a = 2d by
+// r and by rh, d the distance of a pair in range (0 <= d <= r, so a <= 4b; the
+// square root of a float, so +0 or >= 2^-75), with r and rh in [2^-40, 2^40] (the
+// configuration check); a NaN a gives NaN, as the division does.  One input
+// differs: a = -0 gives +0 when yl < 0 (a*yl is then +0), where the division gives
+// -0; the callers never divide -0.  tests/cuda/div_const.cu
+// compares both forms with the IEEE division on every float |a| <= 16b for a set of
+// divisors, bit for bit.
+__device__ __forceinline__ float div_const(float a, float b, float yh, float yl) {
+    const float q0 = __fmaf_rn(a, yh, __fmul_rn(a, yl));
+    const float r = __fmaf_rn(-q0, b, a);
+    return __fmaf_rn(r, yh, q0);
+}
+
+// both scales at once: (a.x / b.x, a.y / b.y), as f32x2 pairs
+__device__ __forceinline__ float2 div_const2(float2 a, float2 b, float2 yh, float2 yl) {
+    const float2 q0 = __ffma2_rn(a, yh, __fmul2_rn(a, yl));
+    const float2 r = __ffma2_rn(make_float2(-q0.x, -q0.y), b, a);
+    return __ffma2_rn(r, yh, q0);
+}
+
+// The reciprocal split of b > 0 for div_const (host).  For floats b and y the
+// product b*y has at most 48 significant bits, so 1 - b*y is exact in double and
+// |1 - b*y| = b*|1/b - y| ranks the three floats around the double reciprocal by
+// their distance to 1/b exactly: yh is the nearest, RN(1/b).
+inline void recip_split(float b, float& yh, float& yl) {
+    const double bd = b;
+    const float y0 = static_cast<float>(1.0 / bd);
+    const float cand[3] = {y0, std::nextafterf(y0, 0.0f), std::nextafterf(y0, INFINITY)};
+    yh = y0;
+    double best = std::fabs(1.0 - bd * static_cast<double>(y0));
+    for (float c : cand) {
+        const double e = std::fabs(1.0 - bd * static_cast<double>(c));
+        if (e < best) {
+            best = e;
+            yh = c;
+        }
+    }
+    yl = static_cast<float>((1.0 - bd * static_cast<double>(yh)) / bd);
+}
 
 // Device-side counters of one solver.  `cur` is what this step's kernels use;
 // `next` is what the step produces; the step's last kernel copies next -> cur.
@@ -126,7 +180,7 @@ struct Kern2 {
 __device__ __forceinline__ Kern2 kern2(float d, const Params& P) {
     Kern2 k;
     const float d2 = d * 2.0f;
-    k.q = make_float2(d2 / P.r, d2 / P.rh);
+    k.q = div_const2(make_float2(d2, d2), make_float2(P.r, P.rh), P.inv_hi, P.inv_lo);  // (d2 / r, d2 / rh)
     k.a = sub2(make_float2(2.0f, 2.0f), k.q);
     k.b = sub2(make_float2(1.0f, 1.0f), k.q);
     k.aa = mul2(k.a, k.a);

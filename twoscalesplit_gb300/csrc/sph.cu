@@ -206,10 +206,11 @@ __global__ void __launch_bounds__(256) k_density_low(Params P0, StepView V) {
 
 // Wall term of a force sum (updateAccCell 562-579 / updateAccCellComplementHigh
 // 867-884): every wall particle of the window's cells, in cell order.  Pairs with
-// sqrtf(x) > rad have q >= 2 and add exactly zero, so they are skipped.
+// sqrtf(x) > rad have q >= 2 and add exactly zero, so they are skipped.  q = 2d/rad
+// through rad's reciprocal split (yh, yl), as in the pair kernels.
 template <class G>
 __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, float2 p, int csx, int cex, int csy,
-                                           int cey, float rad, float Tle, float cB) {
+                                           int cey, float rad, float yh, float yl, float Tle, float cB) {
     float2 accB = make_float2(0.f, 0.f);
     const int* woff = V.woff + P.cbL;
     const float2* wpos = V.wpos + P.wb;
@@ -225,7 +226,8 @@ __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, f
                 return !(x > Tle);  // NaN passes: the reference's 0 * NaN offset propagates it
             },
             [&](int) {
-                const float gm = wall_weight(sqrtf(x), rad, P.cs);
+                const float d = sqrtf(x);
+                const float gm = wall_weight_q(d, div_const(d * 2.0f, rad, yh, yl), P.cs);
                 return make_float2(cB * gm * pik.x, cB * gm * pik.y);
             },
             [](float2& a, float2 t) {
@@ -266,7 +268,7 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
         },
         [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r); },
         add_terms, fl);
-    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.r, P.Tle_r, P.cBL);
+    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.r, P.inv_hi.x, P.inv_lo.x, P.Tle_r, P.cBL);
     PairTerms fh{make_float2(0.f, 0.f), fl.t};  // (accH, accT): the sigma sum continues
     if (cross) {
         grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
@@ -526,7 +528,7 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
         },
         [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx); },
         add_terms, fl);
-    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.rh, P.Tle_rh, P.cBH);
+    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.rh, P.inv_hi.y, P.inv_lo.y, P.Tle_rh, P.cBH);
     float2 acc = fh.a, accL = fl.a;
     const float2 accT = fl.t;
     acc.x *= -P.mH;

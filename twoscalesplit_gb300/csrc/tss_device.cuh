@@ -208,15 +208,19 @@ __device__ __forceinline__ void kernDW2(const Kern2& k, float2 G, float2 x, floa
     gJ = k.q.y < 2.0f ? mul2(make_float2(cJ, cJ), x) : make_float2(0.0f, 0.0f);
 }
 
-// evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114 (selected, as above)
-__device__ __forceinline__ float wall_weight(float d, float rad, float cs) {
-    const float q = d * 2.0f / rad;
+// evaluateBoundaryForceWeight(High), WCSPHSolver.cu:66-114 (selected, as above),
+// at q = 2d / rad
+__device__ __forceinline__ float wall_weight_q(float d, float q, float cs) {
     const float c = 0.02f * cs * cs / (d * d);
     const float r1 = c * 2.0f / 3.0f;
     const float r2 = c * (2.0f * q - 3.0f / 2.0f * q * q);
     const float a = 2.0f - q;
     const float r3 = c * 0.5f * a * a;
     return q < 2.0f / 3.0f ? r1 : (q < 1.0f ? r2 : (q < 2.0f ? r3 : 0.0f));
+}
+
+__device__ __forceinline__ float wall_weight(float d, float rad, float cs) {
+    return wall_weight_q(d, d * 2.0f / rad, cs);
 }
 
 __device__ __forceinline__ float vnorm(float2 v) { return sqrtf(v.x * v.x + v.y * v.y); }

@@ -39,6 +39,21 @@ def test_scene_footprint_is_rounded_to_pages():
     assert f["wall_particles"] == -(-sc.n_wall // _abi.TSS_POOL_WALL_PAGE) * _abi.TSS_POOL_WALL_PAGE
 
 
+@pytest.mark.parametrize("r_low,r_high,ok", [(2.0 ** -40, 2.0 ** -41, False), (2.0 ** -39, 2.0 ** -40, True),
+                                              (2.0 ** 40, 2.0 ** 39, True), (2.0 ** 41, 2.0 ** 40, False),
+                                              (0.01, 0.0, False), (0.01, math.inf, False)])
+def test_support_radii_outside_the_exact_division_range_are_refused(r_low, r_high, ok):
+    """The pair kernels divide by the radii through their reciprocal splits, which is
+    exact for radii in [2^-40, 2^40]; the configuration check refuses the rest."""
+    sc = scenes.mixed_scene(np.random.default_rng(3), n_min=3000, n_max=3001)
+    sc.config.r_low, sc.config.r_high = r_low, r_high
+    if ok:
+        footprint(sc)
+    else:
+        with pytest.raises(_abi.TssError):
+            footprint(sc)
+
+
 def test_pool_bytes_grow_with_capacity_and_budget_fits():
     b1 = pool_bytes(pool_config(1 << 16))
     b2 = pool_bytes(pool_config(1 << 17))

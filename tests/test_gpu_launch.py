@@ -130,6 +130,13 @@ def test_read_positions_equals_download_and_refuses_pageable_memory():
     sol.read_positions(short, high, counts, stream=stream)
     torch.cuda.synchronize()
     assert np.array_equal(short.numpy(), low.numpy()[:3])
+    # a destination 8 bytes past a 16-byte boundary takes the one-entry-per-access path
+    big = torch.zeros((sc.n_low + 1, 2), dtype=torch.float32).pin_memory()
+    shifted = big[1:]
+    assert shifted.data_ptr() % 16 == 8
+    sol.read_positions(shifted, high, counts, stream=stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(shifted.numpy(), low.numpy()) and not big[0].any()
     with pytest.raises(TssError):
         sol.read_positions(torch.zeros((sc.n_low, 2), dtype=torch.float32), high, counts, stream=stream)
 

@@ -130,7 +130,7 @@ def test_read_positions_equals_download_and_refuses_pageable_memory():
     sol.read_positions(short, high, counts, stream=stream)
     torch.cuda.synchronize()
     assert np.array_equal(short.numpy(), low.numpy()[:3])
-    # a destination 8 bytes past a 16-byte boundary takes the one-entry-per-access path
+    # a destination 8 bytes past a 16-byte boundary
     big = torch.zeros((sc.n_low + 1, 2), dtype=torch.float32).pin_memory()
     shifted = big[1:]
     assert shifted.data_ptr() % 16 == 8

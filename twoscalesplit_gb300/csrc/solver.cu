@@ -211,21 +211,6 @@ __global__ void k_set_counts(Counters* c, int nL, int nH) {
 }
 __global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
 
-// n float2 entries from src to dst by the whole grid: two entries per 16-byte
-// access when both addresses allow it (writes to mapped host memory then cross the
-// chip-to-host link in half as many, twice as large transactions), else one per
-// 8-byte access.
-__device__ __forceinline__ void copy_f2(float2* dst, const float2* __restrict__ src, int n) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0) {
-        const int n2 = n >> 1;  // float4 i holds entries 2i and 2i + 1 < n
-        for (int i = t; i < n2; i += stride) reinterpret_cast<float4*>(dst)[i] = reinterpret_cast<const float4*>(src)[i];
-        if ((n & 1) && t == 0) dst[n - 1] = src[n - 1];
-    } else {
-        for (int i = t; i < n; i += stride) dst[i] = src[i];
-    }
-}
-
 // Positions of both lists and their lengths into caller memory (page-locked host
 // memory for tss_solver_read_positions).
 __global__ void k_read_positions(const float2* __restrict__ lowp, const float2* __restrict__ highp,
@@ -236,8 +221,10 @@ __global__ void k_read_positions(const float2* __restrict__ lowp, const float2* 
         counts[0] = nl;
         counts[1] = nh;
     }
-    copy_f2(out_low, lowp, min(nl, cap_low));
-    copy_f2(out_high, highp, min(nh, cap_high));
+    const int ml = min(nl, cap_low), mh = min(nh, cap_high);
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ml; i += stride) out_low[i] = lowp[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < mh; i += stride) out_high[i] = highp[i];
 }
 
 // Key pass of a pool's list: each entry's parameters come from the scene owning

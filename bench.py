@@ -11,8 +11,9 @@ bracketed by CUDA events on the launching stream with L2 flushed (a 512 MiB writ
 between steps.  value = sum over the timed steps of the particles processed
 (n_low + n_high at each step) / device time.  e2e repeats the timed run through
 the C ABI with host buffers: the initial state is uploaded from pinned memory and
-every step's particle positions are read back to pinned memory (an asynchronous
-read-back per step, double-buffered, so the next step runs while the host waits).
+every step's particle positions are read back to pinned memory (an overlapped
+read-back per step, double-buffered: staged on the device, then copied to host
+memory while the next step runs).
 
 With N > 1 (torchrun) every rank runs an independent replica of the scene
 (replicas only: one scene does not shard); value sums the ranks' particle-steps
@@ -368,19 +369,21 @@ def run_ours(args):
     st_avg = {k: v / n_prof for k, v in st_sum.items()}
     # e2e through the C ABI with pinned host buffers: the initial state is uploaded
     # from page-locked memory, and every step's positions (both lists) are read back
-    # into page-locked memory by tss_solver_read_positions, double-buffered: the
-    # host waits for step k's read-back (an event) before it reuses that buffer at
-    # step k + 2, and counts the bytes it received
+    # into page-locked memory by tss_solver_read_positions_async (staged on the
+    # device on the step's stream, then copied to host memory on the solver's own
+    # stream while the next step runs), double-buffered: the host waits for step
+    # k's read-back (its ticket) before it reuses that buffer at step k + 2, and
+    # counts the bytes it received
     reset()
-    sol.step(1, stream=sh)  # keep the graph captured outside the timed region
-    torch.cuda.synchronize(dev)
-    pin_low = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in init_low.items()}
     cap_h = max(sc.cap_high, 1)
     outs = [(torch.empty((sc.n_low, 2), dtype=torch.float32).pin_memory(),
              torch.empty((cap_h, 2), dtype=torch.float32).pin_memory(),
              torch.zeros(2, dtype=torch.int32).pin_memory()) for _ in range(2)]
-    ready = [torch.cuda.Event(), torch.cuda.Event()]
-    pending = [False, False]
+    sol.step(1, stream=sh)  # keep the graph captured and the staging buffers allocated outside the timed region
+    sol.read_wait(sol.read_positions_async(outs[0][0], outs[0][1], outs[0][2], stream=sh))
+    torch.cuda.synchronize(dev)
+    pin_low = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in init_low.items()}
+    tickets = [None, None]
     lib = sol.lib
     st_low = TssScaleState(sc.n_low, _abi.iptr(pin_low["id"].numpy()), fptr(pin_low["pos"].numpy()),
                            fptr(pin_low["vel"].numpy()), _abi.u8ptr(pin_low["state"].numpy()), None, None)
@@ -389,9 +392,9 @@ def run_ours(args):
     h2d = sc.n_low * (4 + 8 + 8 + 1)
 
     def received(b):
-        ready[b].synchronize()
+        sol.read_wait(tickets[b])
         c = outs[b][2].tolist()
-        pending[b] = False
+        tickets[b] = None
         return 8 * (min(c[0], sc.n_low) + min(c[1], cap_h)) + 8
 
     if world > 1:
@@ -402,14 +405,12 @@ def run_ours(args):
     sol.set_fresh(np.zeros(0, np.int32))
     for k in range(K):
         b = k % 2
-        if pending[b]:
+        if tickets[b] is not None:
             d2h += received(b)
         sol.step(1, stream=sh)
-        sol.read_positions(outs[b][0], outs[b][1], outs[b][2], stream=sh)
-        ready[b].record(stream)
-        pending[b] = True
-    for b in range(2):
-        if pending[b]:
+        tickets[b] = sol.read_positions_async(outs[b][0], outs[b][1], outs[b][2], stream=sh)
+    for b in (K % 2, (K + 1) % 2):  # the older read-back first
+        if tickets[b] is not None:
             d2h += received(b)
     e2e_s = time.perf_counter() - e0
     times = torch.tensor([dev_ms, e2e_s, parts], dtype=torch.float64, device=dev)

@@ -79,6 +79,10 @@ def test_status_strings_and_argument_checks(lib):
     assert lib.tss_solver_create(ctypes.byref(c), -1, None, None, 1.0, 0, 1.0, 0, None, 1.0,
                                  ctypes.byref(out)) == _abi.TSS_INVALID_ARG
     assert lib.tss_solver_step(None, 1, None) == _abi.TSS_INVALID_ARG
+    t = ctypes.c_int64(0)
+    assert lib.tss_solver_read_positions_async(None, None, 0, None, 0, None, None, ctypes.byref(t)) == \
+        _abi.TSS_INVALID_ARG
+    assert lib.tss_solver_read_wait(None, 0) == _abi.TSS_INVALID_ARG
 
 
 def test_launch_struct_layout_and_argument_checks(lib, tmp_path):

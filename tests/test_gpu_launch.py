@@ -156,3 +156,53 @@ def test_one_particle_per_warp_through_merges_and_the_guard(relax):
     assert c["total_split"] > 0 and c["total_removed"] > 0
     assert c == ref.counts()
     _assert_same(_state(ref), _state(sol))
+
+
+def test_overlapped_read_back_gives_every_steps_positions():
+    """tss_solver_read_positions_async, two host buffers in turn while the steps go
+    on, against the ordered read-back of the same steps; a later call with larger
+    capacities regrows the staging buffers."""
+    import torch
+    sc = _scene(seed=17, relax=0)
+    stream = torch.cuda.current_stream().cuda_stream
+    ref = Solver.from_scene(sc)
+    want = []
+    lo = torch.zeros((sc.n_low, 2), dtype=torch.float32).pin_memory()
+    hi = torch.zeros((sc.cap_high, 2), dtype=torch.float32).pin_memory()
+    cn = torch.zeros(2, dtype=torch.int32).pin_memory()
+    for _ in range(30):
+        ref.step(1, stream=stream)
+        ref.read_positions(lo, hi, cn, stream=stream)
+        torch.cuda.synchronize()
+        want.append((lo.numpy().copy(), hi.numpy()[:cn[1]].copy(), cn.tolist()))
+    sol = Solver.from_scene(sc)
+    small = 7  # the first calls stage 7 high-res entries at most, later ones all of them
+    bufs = [(torch.zeros((sc.n_low, 2), dtype=torch.float32).pin_memory(),
+             torch.zeros((sc.cap_high, 2), dtype=torch.float32).pin_memory(),
+             torch.zeros(2, dtype=torch.int32).pin_memory()) for _ in range(2)]
+    tickets = [None, None]
+    got = [None] * 30
+
+    def collect(b, k):
+        sol.read_wait(tickets[b])
+        n = bufs[b][2].tolist()
+        m = n[1] if k >= 10 else min(n[1], small)
+        got[k] = (bufs[b][0].numpy().copy(), bufs[b][1].numpy()[:m].copy(), n)
+
+    for k in range(30):
+        b = k % 2
+        if tickets[b] is not None:
+            collect(b, k - 2)
+        sol.step(1, stream=stream)
+        high = bufs[b][1] if k >= 10 else bufs[b][1][:small]
+        tickets[b] = sol.read_positions_async(bufs[b][0], high, bufs[b][2], stream=stream)
+    for k in (28, 29):
+        collect(k % 2, k)
+    assert want[-1][2][1] > small
+    for k in range(30):
+        assert got[k][2] == want[k][2], k
+        assert np.array_equal(got[k][0], want[k][0]), k
+        m = len(got[k][1])
+        assert np.array_equal(got[k][1], want[k][1][:m]), k
+    with pytest.raises(TssError):
+        sol.read_wait(tickets[1] + 1)  # not issued

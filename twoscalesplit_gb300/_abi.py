@@ -260,6 +260,8 @@ def load_library(path=None):
         "tss_solver_profile": (i, [vp, i]),
         "tss_solver_stage_times": (i, [vp, fp, i]),
         "tss_solver_read_positions": (i, [vp, vp, i, vp, i, vp, vp]),
+        "tss_solver_read_positions_async": (i, [vp, vp, i, vp, i, vp, vp, ctypes.POINTER(ctypes.c_int64)]),
+        "tss_solver_read_wait": (i, [vp, ctypes.c_int64]),
         "tss_solver_get_launch": (i, [vp, ctypes.POINTER(TssLaunch)]),
         "tss_solver_set_launch": (i, [vp, ctypes.POINTER(TssLaunch)]),
         "tss_solver_autotune": (i, [vp, i, ctypes.POINTER(TssLaunch), ctypes.POINTER(i)]),

@@ -211,12 +211,13 @@ __global__ void k_set_counts(Counters* c, int nL, int nH) {
 }
 __global__ void k_set_fresh(Counters* c, int n) { c->n_fresh = n; }
 
-// Positions of both lists and their lengths into caller memory (page-locked host
-// memory for tss_solver_read_positions).
+// Positions of both lists and their lengths n[2] into caller memory (page-locked
+// host memory for tss_solver_read_positions; a staging buffer and then host memory
+// for the asynchronous form).
 __global__ void k_read_positions(const float2* __restrict__ lowp, const float2* __restrict__ highp,
-                                 const Counters* __restrict__ c, float2* out_low, int cap_low, float2* out_high,
+                                 const int* __restrict__ n, float2* out_low, int cap_low, float2* out_high,
                                  int cap_high, int* counts) {
-    const int nl = c->cur[0], nh = c->cur[1];
+    const int nl = n[0], nh = n[1];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         counts[0] = nl;
         counts[1] = nh;
@@ -866,15 +867,15 @@ tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n) {
     return TSS_OK;
 }
 
-tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low, float* host_high, int cap_high,
-                                     int* counts, void* stream) {
-    if (!s || !counts || cap_low < 0 || cap_high < 0 || (cap_low > 0 && !host_low) || (cap_high > 0 && !host_high))
+// The device-side addresses of a read-back's page-locked host buffers (an error for
+// memory the GPU cannot reach, which is refused before any kernel touches it).
+static tss_status read_targets(tss_solver* s, float* host_low, int cap_low, float* host_high, int cap_high,
+                               int* counts, void* dev[3]) {
+    if (!counts || cap_low < 0 || cap_high < 0 || (cap_low > 0 && !host_low) || (cap_high > 0 && !host_high))
         return TSS_INVALID_ARG;
-    // the device-side addresses of the page-locked buffers (an error for memory the
-    // GPU cannot reach, which is refused before any kernel touches it)
-    void* dev[3] = {nullptr, nullptr, nullptr};
     void* host[3] = {host_low, host_high, counts};
     for (int k = 0; k < 3; ++k) {
+        dev[k] = nullptr;
         if (!host[k]) continue;
         cudaPointerAttributes a{};
         if (cudaPointerGetAttributes(&a, host[k]) != cudaSuccess || a.type != cudaMemoryTypeHost ||
@@ -883,12 +884,93 @@ tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low
             return s->fail(TSS_INVALID_ARG, "read_positions: host buffers must be page-locked and mapped");
         }
     }
-    const int blocks = std::max(1, std::min(particle_blocks(std::max(cap_low, cap_high), 256), 4 * sm_count()));
-    k_read_positions<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        s->L.npos, s->H.npos, s->cnt, static_cast<float2*>(dev[0]), cap_low, static_cast<float2*>(dev[1]),
+    return TSS_OK;
+}
+
+static int read_blocks(int n) { return std::max(1, std::min(particle_blocks(std::max(n, 1), 256), 4 * sm_count())); }
+
+tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low, float* host_high, int cap_high,
+                                     int* counts, void* stream) {
+    if (!s) return TSS_INVALID_ARG;
+    void* dev[3];
+    const tss_status st = read_targets(s, host_low, cap_low, host_high, cap_high, counts, dev);
+    if (st != TSS_OK) return st;
+    k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        s->L.npos, s->H.npos, &s->cnt->cur[0], static_cast<float2*>(dev[0]), cap_low, static_cast<float2*>(dev[1]),
         cap_high, static_cast<int*>(dev[2]));
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TSS_OK : s->cuda_fail(e, "read_positions");
+}
+
+tss_status tss_solver_read_positions_async(tss_solver* s, float* host_low, int cap_low, float* host_high,
+                                           int cap_high, int* counts, void* stream, int64_t* ticket) {
+    if (!s || !ticket) return TSS_INVALID_ARG;
+    void* dev[3];
+    tss_status st = read_targets(s, host_low, cap_low, host_high, cap_high, counts, dev);
+    if (st != TSS_OK) return st;
+    auto& rb = s->rb;
+    cudaError_t e = cudaSuccess;
+    if (!rb.stream) {  // first call: events and the stream
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+            e = cudaEventCreateWithFlags(&rb.staged[b], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&rb.done[b], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&rb.stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return s->cuda_fail(e, "read_positions_async");
+    }
+    // staging buffers for what the caller reads (a pool's lists can be far longer);
+    // grown when a call asks for more, once the copies in flight are done
+    cap_low = std::min(cap_low, s->nL);
+    cap_high = std::min(cap_high, s->capH);
+    if (!rb.mem || cap_low > rb.cap_low || cap_high > rb.cap_high) {
+        if (rb.mem) {
+            if ((e = cudaStreamSynchronize(rb.stream)) != cudaSuccess) return s->cuda_fail(e, "read_positions_async");
+            cudaFree(rb.mem);
+            rb.mem = nullptr;
+        }
+        rb.cap_low = std::max(rb.cap_low, cap_low);
+        rb.cap_high = std::max(rb.cap_high, cap_high);
+        const size_t per = sizeof(float2) * (static_cast<size_t>(rb.cap_low) + rb.cap_high) + 16;
+        if ((e = cudaMalloc(&rb.mem, 2 * per)) != cudaSuccess) {
+            rb.cap_low = rb.cap_high = 0;
+            return s->cuda_fail(e, "read_positions_async");
+        }
+        for (int b = 0; b < 2; ++b) {
+            char* base = static_cast<char*>(rb.mem) + b * per;
+            rb.counts[b] = reinterpret_cast<int*>(base);
+            rb.low[b] = reinterpret_cast<float2*>(base + 16);
+            rb.high[b] = rb.low[b] + rb.cap_low;
+        }
+    }
+    const int b = static_cast<int>(rb.issued & 1);
+    const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    // the buffer's previous host copy (two calls ago) must be done before it is refilled
+    if (rb.issued >= 2) e = cudaStreamWaitEvent(cs, rb.done[b], 0);
+    if (e == cudaSuccess) {
+        k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, cs>>>(
+            s->L.npos, s->H.npos, &s->cnt->cur[0], rb.low[b], cap_low, rb.high[b], cap_high, rb.counts[b]);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(rb.staged[b], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(rb.stream, rb.staged[b], 0);
+    if (e == cudaSuccess) {
+        k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, rb.stream>>>(
+            rb.low[b], rb.high[b], rb.counts[b], static_cast<float2*>(dev[0]), cap_low, static_cast<float2*>(dev[1]),
+            cap_high, static_cast<int*>(dev[2]));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(rb.done[b], rb.stream);
+    if (e != cudaSuccess) return s->cuda_fail(e, "read_positions_async");
+    *ticket = rb.issued++;
+    return TSS_OK;
+}
+
+tss_status tss_solver_read_wait(tss_solver* s, int64_t ticket) {
+    if (!s || ticket < 0 || ticket >= s->rb.issued) return TSS_INVALID_ARG;
+    // buffer ticket & 1 was last used by ticket or a later read-back on the same
+    // in-order stream: its completion implies this one's
+    const cudaError_t e = cudaEventSynchronize(s->rb.done[ticket & 1]);
+    return e == cudaSuccess ? TSS_OK : s->cuda_fail(e, "read_wait");
 }
 
 tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out) {

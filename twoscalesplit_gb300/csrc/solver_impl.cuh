@@ -151,6 +151,20 @@ struct tss_solver {
     int capW = 0;
     void* render_ws = nullptr;           // tss_solver_render scratch, allocated at its first call
     size_t render_ws_bytes = 0;
+    // tss_solver_read_positions_async, set up at its first call: two staging
+    // buffers used in turn (positions of both lists and their lengths) and a stream
+    // for the copies from them to host memory
+    struct ReadBack {
+        cudaStream_t stream = nullptr;
+        void* mem = nullptr;
+        float2* low[2] = {};
+        float2* high[2] = {};
+        int* counts[2] = {};
+        cudaEvent_t staged[2] = {};  // on the caller's stream: the staging copy is done
+        cudaEvent_t done[2] = {};    // on rb.stream: the host copy is done (the buffer is free)
+        int64_t issued = 0;          // tickets handed out; ticket t used buffer t & 1
+        int cap_low = 0, cap_high = 0;  // entries each staging buffer holds per list
+    } rb;
 
     tss_status fail(tss_status st, const std::string& msg) {
         err = msg;
@@ -184,5 +198,12 @@ struct tss_solver {
         if (stream) cudaStreamDestroy(stream);
         if (arena) cudaFree(arena);
         if (render_ws) cudaFree(render_ws);
+        if (rb.stream) cudaStreamSynchronize(rb.stream);
+        for (int b = 0; b < 2; ++b) {
+            if (rb.staged[b]) cudaEventDestroy(rb.staged[b]);
+            if (rb.done[b]) cudaEventDestroy(rb.done[b]);
+        }
+        if (rb.stream) cudaStreamDestroy(rb.stream);
+        if (rb.mem) cudaFree(rb.mem);
     }
 };

@@ -133,6 +133,21 @@ class Solver:
             ctypes.c_void_p(host_high.data_ptr()), int(host_high.shape[0]), ctypes.c_void_p(counts.data_ptr()),
             ctypes.c_void_p(stream) if stream else None))
 
+    def read_positions_async(self, host_low, host_high, counts, stream=None):
+        """The read-back overlapped with the following steps
+        (tss_solver_read_positions_async): returns a ticket; read the buffers after
+        read_wait(ticket)."""
+        t = ctypes.c_int64(0)
+        self._check(self.lib.tss_solver_read_positions_async(
+            self.h, ctypes.c_void_p(host_low.data_ptr()), int(host_low.shape[0]),
+            ctypes.c_void_p(host_high.data_ptr()), int(host_high.shape[0]), ctypes.c_void_p(counts.data_ptr()),
+            ctypes.c_void_p(stream) if stream else None, ctypes.byref(t)))
+        return t.value
+
+    def read_wait(self, ticket):
+        """Blocks until the read-back with this ticket has written host memory."""
+        self._check(self.lib.tss_solver_read_wait(self.h, ctypes.c_int64(ticket)))
+
     @property
     def launch(self):
         """Launch shape of the gathers: {gather: {"threads": t, "persistent": bool}}."""

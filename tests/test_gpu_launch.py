@@ -206,3 +206,29 @@ def test_overlapped_read_back_gives_every_steps_positions():
         assert np.array_equal(got[k][1], want[k][1][:m]), k
     with pytest.raises(TssError):
         sol.read_wait(tickets[1] + 1)  # not issued
+
+
+def test_overlapped_read_back_of_a_batch():
+    """A batch's list lengths are on the device only: its overlapped read-back goes
+    by kernel for both lists and must equal the ordered one."""
+    import torch
+    scs = [_scene(seed=s, relax=0) for s in (21, 22)]
+    stream = torch.cuda.current_stream().cuda_stream
+    a, b = Batch(scs), Batch(scs)
+    n_low = sum(sc.n_low for sc in scs)
+    cap_h = sum(sc.cap_high for sc in scs)
+    bufs = [(torch.zeros((n_low, 2), dtype=torch.float32).pin_memory(),
+             torch.zeros((cap_h, 2), dtype=torch.float32).pin_memory(),
+             torch.zeros(2, dtype=torch.int32).pin_memory()) for _ in range(2)]
+    for k in range(12):
+        a.step(1, stream=stream)
+        b.step(1, stream=stream)
+        a.read_positions(bufs[0][0], bufs[0][1], bufs[0][2], stream=stream)
+        t = b.read_positions_async(bufs[1][0], bufs[1][1], bufs[1][2], stream=stream)
+        b.read_wait(t)
+        torch.cuda.synchronize()
+        n = bufs[0][2].tolist()
+        assert bufs[1][2].tolist() == n
+        assert np.array_equal(bufs[0][0].numpy(), bufs[1][0].numpy())
+        assert np.array_equal(bufs[0][1].numpy()[:n[1]], bufs[1][1].numpy()[:n[1]])
+    assert n[1] > 0

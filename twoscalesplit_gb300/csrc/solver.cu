@@ -953,10 +953,19 @@ tss_status tss_solver_read_positions_async(tss_solver* s, float* host_low, int c
     }
     if (e == cudaSuccess) e = cudaEventRecord(rb.staged[b], cs);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(rb.stream, rb.staged[b], 0);
+    // A single scene's low-res list always holds all nL particles, so its length is
+    // known here and a copy engine moves it, leaving the SMs to the next step; the
+    // high-res list (its length is on the device) and the lengths go by a kernel.
+    int kernel_low = cap_low;
+    if (e == cudaSuccess && !s->batched && cap_low > 0) {
+        e = cudaMemcpyAsync(host_low, rb.low[b], sizeof(float2) * static_cast<size_t>(cap_low),
+                            cudaMemcpyDeviceToHost, rb.stream);
+        kernel_low = 0;
+    }
     if (e == cudaSuccess) {
-        k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, rb.stream>>>(
-            rb.low[b], rb.high[b], rb.counts[b], static_cast<float2*>(dev[0]), cap_low, static_cast<float2*>(dev[1]),
-            cap_high, static_cast<int*>(dev[2]));
+        k_read_positions<<<read_blocks(std::max(kernel_low, cap_high)), 256, 0, rb.stream>>>(
+            rb.low[b], rb.high[b], rb.counts[b], static_cast<float2*>(dev[0]), kernel_low,
+            static_cast<float2*>(dev[1]), cap_high, static_cast<int*>(dev[2]));
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaEventRecord(rb.done[b], rb.stream);

@@ -1,13 +1,15 @@
 // div_const / div_const2 (division by a per-scene constant through its reciprocal
 // split, tss_device.cuh) against the IEEE division, bit for bit, on EVERY float a
-// with 2^-75 <= |a| <= 16b and on a = +0 (-0, which the kernels never divide, may
-// come out +0), for each divisor b: the smoothing
-// lengths of the library's workloads, the ends of the accepted radius range
-// [2^-40, 2^40], and 48 seeded log-uniform divisors in that range.  The pair
-// kernels divide a = 2d <= 4b, d = 0 or the square root of a positive float
-// (>= 2^-74.5).
+// with 2^-75 <= |a| <= 2^20 b and on a = +0 (-0, which the kernels never divide,
+// may come out +0), for each divisor b: the smoothing lengths of the library's
+// workloads, the ends of the accepted radius range [2^-40, 2^40], and 48 seeded
+// log-uniform divisors in that range.  The pair kernels divide a = 2d <= 4b, d = 0
+// or the square root of a positive float (>= 2^-74.5); the grid coordinates divide
+// a position's offset from the origin, whose quotient is a cell coordinate (grids
+// of up to 2^20 cells a side are covered).
 // Prints "mismatches <count> of <checked>" (and the first mismatch); exits 0
 // unless a CUDA call fails.  The kernel touches no memory but two counters.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -61,7 +63,7 @@ int main() {
     for (float b : bs) {
         float yh, yl;
         recip_split(b, yh, yl);
-        const float lim = 16.0f * b;
+        const float lim = std::ldexp(b, 20);
         unsigned hi;
         std::memcpy(&hi, &lim, sizeof(hi));
         cudaMemset(d_bad, 0, sizeof(unsigned long long));

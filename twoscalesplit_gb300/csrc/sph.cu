@@ -58,8 +58,8 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
     float x = 0.0f;
     const auto term = [&](int) { return pair_density(P, sqrtf(x)); };
     int csx, csy, cex, cey;
-    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
+    grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
     G::window(
         offH, P.dimH[0], csx, cex, csy, cey,
         [&](int k) {
@@ -68,8 +68,8 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
             return x <= P.Tle_rh;
         },
         term, add_density, d);
-    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
+    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     if (P.q1) {
         // The reference reads the HIGH sorted list at LOW-grid ranges of its own
         // scene; past the scene's n_high that list still holds its initial identity
@@ -158,8 +158,8 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
     float x = 0.0f;
     const auto term = [&](int) { return pair_density(P, sqrtf(x)); };
     int csx, csy, cex, cey;
-    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
+    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     G::window(
         L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
         [&](int k) {
@@ -168,8 +168,8 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
         },
         term, add_density, d);
     if (cross) {  // only state-0 high-res particles can contribute (lambda_LH)
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        grid_coord_s<1>(P, p.x, p.y, -P.r, csx, csy);
+        grid_coord_s<1>(P, p.x, p.y, P.r, cex, cey);
         G::window(
             H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
             [&](int k) {
@@ -257,8 +257,8 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     float2 pij = make_float2(0.f, 0.f);
     float x = 0.0f;
     int csx, csy, cex, cey;
-    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
+    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     G::window(
         L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
         [&](int k) {
@@ -271,8 +271,8 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.r, P.inv_hi.x, P.inv_lo.x, P.Tle_r, P.cBL);
     PairTerms fh{make_float2(0.f, 0.f), fl.t};  // (accH, accT): the sigma sum continues
     if (cross) {
-        grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-        grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+        grid_coord_s<1>(P, p.x, p.y, -P.r, csx, csy);
+        grid_coord_s<1>(P, p.x, p.y, P.r, cex, cey);
         G::window(
             H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
             [&](int k) {
@@ -323,7 +323,7 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
         L.nvel[i] = v;
         L.nid[i] = L.id[i];
         grid_key(L.gcount, L.gkey, L.grank, L.gtile, i,
-                 P.cbL + cell_hash(p, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1]));
+                 P.cbL + cell_hash_s<0>(P, p));
         L.nst[i] = ns;
         V.split_flag[i] = flag ? 1 : 0;
         if (L.ndens) {
@@ -390,7 +390,7 @@ __device__ __forceinline__ void make_children(const Params& P, const StepView& V
         V.H.nst[h] = 1;
         V.H.nid[h] = 4 * id + c;
         grid_key(V.H.gcount, V.H.gkey, V.H.grank, V.H.gtile, h,
-                 P.cbH + cell_hash(cp[c], P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
+                 P.cbH + cell_hash_s<1>(P, cp[c]));
         if (V.H.ndens) {
             V.H.ndens[h] = 0.0f;
             V.H.npres[h] = 0.0f;
@@ -503,8 +503,8 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     float2 pij = make_float2(0.f, 0.f);
     float x = 0.0f;
     int csx, csy, cex, cey;
-    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
+    grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
     G::window(
         H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
         [&](int k) {
@@ -515,8 +515,8 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
         },
         [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh); },
         add_terms, fh);
-    grid_coord(p.x, p.y, -P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-    grid_coord(p.x, p.y, P.r, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
+    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     PairTerms fl{make_float2(0.f, 0.f), fh.t};  // (accL, accT): the sigma sum continues
     G::window(
         L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
@@ -581,7 +581,7 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
         H.map[id] = -1;
         atomicAdd(&V.cnt->n_drop, 1);
     } else {
-        grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, P.cbH + cell_hash(p, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1]));
+        grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, P.cbH + cell_hash_s<1>(P, p));
     }
     if (H.ndens) {
         H.ndens[i] = dens;
@@ -625,8 +625,8 @@ __device__ __forceinline__ void relax_density_one(const Params& P, const StepVie
     const float2 p = H.pos[i];
     float d = 0.0f, dl = 0.0f;
     int csx, csy, cex, cey;
-    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
+    grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimH[0];
         const int b = offH[row + cex + 1];
@@ -635,8 +635,8 @@ __device__ __forceinline__ void relax_density_one(const Params& P, const StepVie
             if (dist <= P.rh) d += kernW(dist, P.rh, P.CH);
         }
     }
-    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    grid_coord_s<0>(P, p.x, p.y, -P.rh, csx, csy);
+    grid_coord_s<0>(P, p.x, p.y, P.rh, cex, cey);
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimL[0];
         const int b = offL[row + cex + 1];
@@ -679,8 +679,8 @@ __device__ __forceinline__ void relax_force_one(const Params& P, const StepView&
     const float dens2 = dens * dens;
     float2 acc = make_float2(0.f, 0.f), accL = make_float2(0.f, 0.f), accB = make_float2(0.f, 0.f);
     int csx, csy, cex, cey;
-    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], csx, csy);
-    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.rh, P.dimH[0], P.dimH[1], cex, cey);
+    grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
+    grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimH[0];
         const int b = offH[row + cex + 1];
@@ -696,8 +696,8 @@ __device__ __forceinline__ void relax_force_one(const Params& P, const StepView&
             }
         }
     }
-    grid_coord(p.x, p.y, -P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], csx, csy);
-    grid_coord(p.x, p.y, P.rh, P.ox, P.oy, P.r, P.dimL[0], P.dimL[1], cex, cey);
+    grid_coord_s<0>(P, p.x, p.y, -P.rh, csx, csy);
+    grid_coord_s<0>(P, p.x, p.y, P.rh, cex, cey);
     for (int cy = csy; cy <= cey; ++cy) {
         const int row = cy * P.dimL[0];
         const int b = offL[row + cex + 1];

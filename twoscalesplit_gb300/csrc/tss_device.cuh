@@ -145,6 +145,35 @@ __device__ __forceinline__ int cell_hash(float2 p, float ox, float oy, float cel
     return cy * dimx + cx;
 }
 
+// computeGridCoordinate on grid S of a scene (0: the low-res grid, cell r; 1: the
+// high-res grid, cell rh), the quotient by the cell size taken with div_const.  A
+// cell index needs only the truncation of the IEEE quotient, and div_const gives
+// that for every finite a: it is the IEEE quotient for 2^-75 <= |a| (the quotient
+// then normal), and for smaller |a| both quotients are below 2^-35 and truncate
+// to 0.  An infinite or NaN a keeps the division's result, a itself (the cell size
+// is positive and finite).
+__device__ __forceinline__ float cell_quot(float a, float cell, float yh, float yl) {
+    return isfinite(a) ? div_const(a, cell, yh, yl) : a;
+}
+
+template <int S>
+__device__ __forceinline__ void grid_coord_s(const Params& P, float px, float py, float off, int& cx, int& cy) {
+    const float cell = S ? P.rh : P.r;
+    const float yh = S ? P.inv_hi.y : P.inv_hi.x, yl = S ? P.inv_lo.y : P.inv_lo.x;
+    const int dimx = S ? P.dimH[0] : P.dimL[0], dimy = S ? P.dimH[1] : P.dimL[1];
+    cx = f2i(cell_quot((px + off) - P.ox, cell, yh, yl));
+    cy = f2i(cell_quot((py + off) - P.oy, cell, yh, yl));
+    cx = min(max(0, cx), dimx - 1);
+    cy = min(max(0, cy), dimy - 1);
+}
+
+template <int S>
+__device__ __forceinline__ int cell_hash_s(const Params& P, float2 p) {
+    int cx, cy;
+    grid_coord_s<S>(P, p.x, p.y, 0.0f, cx, cy);
+    return cy * (S ? P.dimH[0] : P.dimL[0]) + cx;
+}
+
 // evaluateM4Kernel(High), WCSPHSolver.cu:116-160.  Both polynomial branches are
 // evaluated and one is selected: each branch's expression keeps the reference's
 // association, so the selected value is the reference's bit for bit, and a warp

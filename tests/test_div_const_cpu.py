@@ -21,7 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def rn32(x):
-    """x (a Fraction) rounded to the nearest FP32 value, ties to even (normal range)."""
+    """x (a Fraction) rounded to the nearest FP32 value, ties to even (subnormals
+    included: below 2^-126 the spacing is 2^-149)."""
     if x == 0:
         return 0.0
     s = -1 if x < 0 else 1
@@ -31,8 +32,9 @@ def rn32(x):
         e -= 1
     while Fraction(2) ** (e + 1) <= x:
         e += 1
-    assert -126 <= e <= 127
-    m = x / Fraction(2) ** (e - 23)  # in [2^23, 2^24)
+    assert e <= 127
+    e = max(e, -126)
+    m = x / Fraction(2) ** (e - 23)  # in [2^23, 2^24) for normal results
     q, r = divmod(m.numerator, m.denominator)
     if 2 * r > m.denominator or (2 * r == m.denominator and q % 2 == 1):
         q += 1
@@ -92,3 +94,17 @@ def test_division_steps_give_the_correctly_rounded_quotient(splits):
             assert got == want, (a.hex(), b.hex(), got, want)
             checked += 1
     assert checked > 15000
+
+
+def test_cell_coordinates_of_tiny_offsets_truncate_to_zero(splits):
+    """The grid coordinates use the same steps (cell_quot).  Below |a| = 2^-75 they
+    may leave the normal range, but the quotient stays far below 1 in magnitude,
+    so its truncation -- the cell index -- is 0, as the IEEE quotient's is."""
+    rng = np.random.default_rng(9)
+    for b, yh, yl in splits[::5]:
+        for a in list(np.exp2(rng.uniform(-149, -75, 40))) + [2.0 ** -149, 2.0 ** -76]:
+            a = f32(float(a))
+            for sa in (a, -a):
+                got = div_const(sa, b, yh, yl)
+                want = rn32(Fraction(sa) / Fraction(b))
+                assert abs(got) < 2.0 ** -30 and int(got) == int(want) == 0, (sa, b)

@@ -108,3 +108,24 @@ def test_cell_coordinates_of_tiny_offsets_truncate_to_zero(splits):
                 got = div_const(sa, b, yh, yl)
                 want = rn32(Fraction(sa) / Fraction(b))
                 assert abs(got) < 2.0 ** -30 and int(got) == int(want) == 0, (sa, b)
+
+
+def cell_quot(a, b, yh, yl):
+    """tss_device.cuh cell_quot: finite offsets through the division steps,
+    infinite and NaN ones passed through."""
+    return div_const(a, b, yh, yl) if math.isfinite(a) else a
+
+
+def test_cell_coordinates_beyond_the_exhaustive_range(splits):
+    """Grid coordinates between 2^20 and 2^31 cells (past the GPU test's exhaustive
+    range; the clamp to the grid only reads them there) truncate as the IEEE
+    quotient does, and infinite or NaN offsets give the division's own result."""
+    rng = np.random.default_rng(13)
+    for b, yh, yl in splits[::3]:
+        for a in b * np.exp2(rng.uniform(20, 31, 25)):
+            for sa in (f32(float(a)), -f32(float(a))):
+                got = cell_quot(sa, b, yh, yl)
+                assert got == rn32(Fraction(sa) / Fraction(b)), (sa, b)
+        assert cell_quot(math.inf, b, yh, yl) == math.inf
+        assert cell_quot(-math.inf, b, yh, yl) == -math.inf
+        assert math.isnan(cell_quot(math.nan, b, yh, yl))

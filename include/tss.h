@@ -29,7 +29,9 @@ typedef enum tss_status {
     TSS_CUDA_ERROR = 3,    /* a CUDA runtime call failed                          */
     TSS_CAPACITY = 4,      /* a particle pool would overflow its capacity         */
     TSS_NUMERIC = 5,       /* NaN/Inf in a density, pressure or acceleration      */
-    TSS_TIMEOUT = 6,       /* a bounded device-side wait gave up                  */
+    TSS_GRID_INDEX = 6,    /* a grid index check failed: inconsistent cell offsets */
+                           /* (the affected entries were skipped, nothing written  */
+                           /* outside a buffer)                                    */
     TSS_NO_DEVICE = 7      /* no CUDA device                                      */
 } tss_status;
 
@@ -291,7 +293,7 @@ tss_status tss_server_last_error(tss_server* sv, char* buf, int len);
 tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream);
 
 /* Block until all enqueued work is done; returns the device error word mapped to a
- * status (TSS_CAPACITY, TSS_NUMERIC, TSS_TIMEOUT) or TSS_OK. */
+ * status (TSS_CAPACITY, TSS_NUMERIC, TSS_GRID_INDEX) or TSS_OK. */
 tss_status tss_solver_sync(tss_solver* s);
 
 typedef struct tss_counts {
@@ -308,7 +310,7 @@ typedef struct tss_counts {
 
 #define TSS_ERR_CAPACITY 0x1u /* a split would overflow the high-res pool            */
 #define TSS_ERR_NUMERIC  0x2u /* NaN/Inf density, pressure or acceleration            */
-#define TSS_ERR_TIMEOUT  0x4u /* a bounded device-side wait gave up                   */
+#define TSS_ERR_GRID_INDEX 0x4u /* a grid index check failed (inconsistent offsets)  */
 
 tss_status tss_solver_counts(tss_solver* s, tss_counts* out);
 
@@ -432,6 +434,24 @@ tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in);
  * gather keeps the default shape unless a candidate is more than 5% faster on the
  * trial steps.  Synchronises. */
 tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* best, int* steps_taken);
+
+/* Arithmetic of the gathers' pair terms.  TSS_ARITH_EXACT (the default) is the
+ * reference's FP32 arithmetic: IEEE square root and division, no fused
+ * multiply-adds, the reference's association, so results equal the reference's
+ * bit for bit for the same list order.  TSS_ARITH_FAST spends the step's tolerance
+ * (densities, forces and positions within 1e-5 relative in FP32) instead: one
+ * approximate reciprocal square root and one approximate reciprocal per pair,
+ * fused multiply-adds, the cubic spline and its gradient in expanded form.  The
+ * neighbour sets, summation order, cutoffs, grid and split logic are the same in
+ * both; only the per-pair values differ, by a few units in the last place, so a
+ * split decision can differ only for a particle within rounding of the region's
+ * edge.  The reference has no counterpart (its Release build used IEEE arithmetic,
+ * WCSPHSolver.cu.cache's FastMath=false).  Applies to every scene of a handle; the
+ * step graphs are captured again at the next step. */
+#define TSS_ARITH_EXACT 0
+#define TSS_ARITH_FAST 1
+tss_status tss_solver_set_arith(tss_solver* s, int mode);
+tss_status tss_solver_get_arith(tss_solver* s, int* mode);
 
 /* Last error message of this handle (NUL-terminated, truncated to len). */
 tss_status tss_solver_last_error(tss_solver* s, char* buf, int len);

@@ -19,10 +19,10 @@ TSS_OOM = 2
 TSS_CUDA_ERROR = 3
 TSS_CAPACITY = 4
 TSS_NUMERIC = 5
-TSS_TIMEOUT = 6
+TSS_GRID_INDEX = 6
 TSS_NO_DEVICE = 7
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "CAPACITY",
-                5: "NUMERIC", 6: "TIMEOUT", 7: "NO_DEVICE"}
+                5: "NUMERIC", 6: "GRID_INDEX", 7: "NO_DEVICE"}
 
 TSS_FLAG_Q1_COMPAT = 0x1
 TSS_FLAG_MERGE = 0x2
@@ -48,7 +48,9 @@ GATHER_NAMES = ["density_high", "density_low", "force_low", "force_high"]
 TSS_ERR_CAPACITY = 0x1
 TSS_GRID_NOALLOC_MAX_BYTES = 32 << 20
 TSS_ERR_NUMERIC = 0x2
-TSS_ERR_TIMEOUT = 0x4
+TSS_ERR_GRID_INDEX = 0x4
+TSS_ARITH_EXACT = 0
+TSS_ARITH_FAST = 1
 
 
 class TssError(RuntimeError):
@@ -265,6 +267,8 @@ def load_library(path=None):
         "tss_solver_get_launch": (i, [vp, ctypes.POINTER(TssLaunch)]),
         "tss_solver_set_launch": (i, [vp, ctypes.POINTER(TssLaunch)]),
         "tss_solver_autotune": (i, [vp, i, ctypes.POINTER(TssLaunch), ctypes.POINTER(i)]),
+        "tss_solver_set_arith": (i, [vp, i]),
+        "tss_solver_get_arith": (i, [vp, ctypes.POINTER(i)]),
         "tss_status_string": (ctypes.c_char_p, [i]),
         "tss_grid_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
         "tss_batch_create": (i, [i, ctypes.POINTER(TssSceneDesc), i, ctypes.POINTER(vp)]),

@@ -13,8 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtss.so")
-SOURCES = ["grid.cu", "grid_noalloc.cu", "sph.cu", "solver.cu", "pool.cu", "render.cu", "serve.cpp"]
-HEADERS = ["tss_device.cuh", "gather.cuh", "grid.cuh", "sph.cuh", "solver_impl.cuh", "extent.hpp"]
+SOURCES = ["grid.cu", "grid_noalloc.cu", "sph.cu", "sph_fast.cu", "solver.cu", "pool.cu", "render.cu", "serve.cpp"]
+HEADERS = ["tss_device.cuh", "arith.cuh", "gather.cuh", "gathers.cuh", "grid.cuh", "sph.cuh", "solver_impl.cuh",
+           "extent.hpp"]
 ARCH = os.environ.get("TSS_CUDA_ARCH", "103a")
 
 

@@ -140,9 +140,9 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
     }
 }
 
-// Every index below is checked: if a look-back wait gave up (kErrTimeout) the
-// offsets may be inconsistent, and the build then skips entries instead of
-// touching memory outside its buffers.
+// Every index below is checked: offsets that do not fit the keys or ranks (a
+// caller's table, ids that are not distinct) set kErrGridIndex, and the build then
+// skips those entries instead of touching memory outside its buffers.
 __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __restrict__ id, GridBufs g,
                                unsigned* err) {
     const int n = *n_ptr;
@@ -151,12 +151,12 @@ __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __r
         const int c = g.key[i];
         if (c < 0) continue;  // dropped from the list
         if (c >= g.ncells) {
-            atomicOr(err, kErrTimeout);
+            atomicOr(err, kErrGridIndex);
             continue;
         }
         const int dst = g.off[c] + g.rank[i];
         if (dst < 0 || dst >= total) {
-            atomicOr(err, kErrTimeout);
+            atomicOr(err, kErrGridIndex);
             continue;
         }
         g.perm[dst] = make_int2(i, id[i]);
@@ -172,17 +172,17 @@ __global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, u
         int2 pe = g.perm[k];
         const int src = pe.x, id = pe.y;
         if (src < 0 || src >= cap) {
-            atomicOr(err, kErrTimeout);
+            atomicOr(err, kErrGridIndex);
             continue;
         }
         const int c = g.key[src];
         if (c < 0 || c >= g.ncells) {
-            atomicOr(err, kErrTimeout);
+            atomicOr(err, kErrGridIndex);
             continue;
         }
         const int s = g.off[c], e = g.off[c + 1];
         if (s < 0 || e > n || s > k || k >= e) {
-            atomicOr(err, kErrTimeout);
+            atomicOr(err, kErrGridIndex);
             continue;
         }
         int r = 0;
@@ -204,7 +204,7 @@ __global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, u
         if (a.dst_sc) a.dst_sc[dst] = a.page_scene[(id >> a.id_shift) >> a.page_shift];
         if (a.slot_map) {
             if (id >= 0 && id < a.slots) a.slot_map[id] = dst;
-            else atomicOr(err, kErrTimeout);
+            else atomicOr(err, kErrGridIndex);
         }
     }
 }

@@ -82,7 +82,7 @@ __global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, u
 
 // Enqueue a whole build: clears the counts and tile sums, then keys, scan,
 // scatter, reorder.  `n_ptr` is a device int <= cap; inconsistent offsets set
-// kErrTimeout in *err.
+// kErrGridIndex in *err.
 cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, int* n_ptr, int cap, float ox, float oy,
                                float cell, int dimx, int dimy, GridBufs g, ReorderArgs a, unsigned* err,
                                cudaStream_t stream);

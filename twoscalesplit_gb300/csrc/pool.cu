@@ -540,7 +540,12 @@ tss_status tss_pool_create(const tss_pool_config* cfg, tss_solver** out) {
 
 tss_status tss_pool_admit(tss_solver* s, const tss_scene_desc* scene, void* stream, int* scene_id) {
     if (!s || !scene || !scene_id || !s->batched) return TSS_INVALID_ARG;
-    return admit(s, scene_in(*scene), static_cast<cudaStream_t>(stream), scene_id);
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = s->enter(st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "admit");
+    const tss_status r = admit(s, scene_in(*scene), st, scene_id);
+    if ((e = s->leave(st)) != cudaSuccess) return s->cuda_fail(e, "admit");
+    return r;
 }
 
 tss_status tss_pool_can_admit(tss_solver* s, const tss_scene_desc* scene) {
@@ -551,6 +556,8 @@ tss_status tss_pool_can_admit(tss_solver* s, const tss_scene_desc* scene) {
 tss_status tss_pool_retire(tss_solver* s, int id, void* stream) {
     if (!s || !s->batched || id < 0 || id >= s->S || !s->scenes[id].live) return TSS_INVALID_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = s->enter(st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "retire");
     SceneRec& r = s->scenes[id];
     const int lo = static_cast<int>(r.sb), hi = static_cast<int>(r.sb + r.n_low);
     k_retire<<<s->blocksL, 256, 0, st>>>(s->L.nid, &s->cnt->cur[0], s->nL, 0, lo, hi, s->L.g, nullptr, 0);
@@ -568,7 +575,8 @@ tss_status tss_pool_retire(tss_solver* s, int id, void* stream) {
     r.live = false;
     s->free_ids.push_back(id);
     std::sort(s->free_ids.begin(), s->free_ids.end(), std::greater<int>());  // lowest id on top
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = s->leave(st);
     if (e != cudaSuccess) return s->cuda_fail(e, "retire");
     return TSS_OK;
 }
@@ -591,7 +599,8 @@ tss_status tss_pool_extract(tss_solver* s, int id, const tss_scene_result* dst, 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const Params& P = s->h_table[id];
     const int CLs = P.dimL[0] * P.dimL[1];
-    cudaError_t e = cudaMemsetAsync(s->ext_cnt, 0, 2 * sizeof(unsigned), st);
+    cudaError_t e = s->enter(st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->ext_cnt, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return s->cuda_fail(e, "extract");
     k_count_splits<<<particle_blocks(static_cast<int>(std::max<int64_t>(s->live_low, 1)), 256), 256, 0, st>>>(
         s->split_flag, s->L.g.off, P.cbL, CLs, s->cnt, s->ext_cnt, d_counts);
@@ -622,7 +631,8 @@ tss_status tss_pool_extract(tss_solver* s, int id, const tss_scene_result* dst, 
     a.dst = *dst;
     a.d_counts = d_counts;
     k_extract<<<particle_blocks(static_cast<int>(std::min<int64_t>(5 * r.n_low, 1 << 30)), 256), 256, 0, st>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return s->cuda_fail(e, "extract");
+    if ((e = cudaGetLastError()) == cudaSuccess) e = s->leave(st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "extract");
     return TSS_OK;
 }
 
@@ -703,7 +713,7 @@ tss_status tss_solver_scene_counts(tss_solver* s, int* n_low, int* n_high) {
         for (int k = 0; k < ns; ++k) n_low[k] = s->scenes[k].live ? static_cast<int>(s->scenes[k].n_low) : 0;
     if (n_high) {
         std::vector<int32_t> ids(static_cast<size_t>(c.n_high));
-        cudaError_t e = c.n_high ? cudaMemcpy(ids.data(), s->H.nid, sizeof(int32_t) * c.n_high, cudaMemcpyDeviceToHost)
+        cudaError_t e = c.n_high ? s->d2h(ids.data(), s->H.nid, sizeof(int32_t) * c.n_high)
                                  : cudaSuccess;
         if (e != cudaSuccess) return s->cuda_fail(e, "scene counts");
         for (int k = 0; k < ns; ++k) n_high[k] = 0;

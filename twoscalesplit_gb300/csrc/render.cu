@@ -339,13 +339,14 @@ tss_status tss_solver_render(tss_solver* s, const tss_view* v, const float* poin
     size_t need = 0;
     for (int k = 0; k < 3; ++k) need = std::max(need, ws_size(entries_cap(caps[k], v, point_sizes[k]), v->width, v->height));
     need += 256;
+    cudaError_t e = s->enter(st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "render");
     if (need > s->render_ws_bytes) {
-        cudaStreamSynchronize(st);
+        if ((e = s->wait_idle()) != cudaSuccess) return s->cuda_fail(e, "render");
         if (s->render_ws) cudaFree(s->render_ws);
         s->render_ws = nullptr;
         s->render_ws_bytes = 0;
-        cudaError_t e = cudaMalloc(&s->render_ws, need);
-        if (e != cudaSuccess) return s->cuda_fail(e, "render workspace");
+        if ((e = cudaMalloc(&s->render_ws, need)) != cudaSuccess) return s->cuda_fail(e, "render workspace");
         s->render_ws_bytes = need;
     }
     char* w = static_cast<char*>(s->render_ws);
@@ -359,7 +360,7 @@ tss_status tss_solver_render(tss_solver* s, const tss_view* v, const float* poin
     // densities of the last step are valid for the list entries it sorted
     const int* valid[2] = {s->carry ? nullptr : &s->cnt->sorted[0], s->carry ? nullptr : &s->cnt->sorted[1]};
     const float* dens[2] = {s->carry ? s->L.ndens : s->L.dens, s->carry ? s->H.ndens : s->H.dens};
-    cudaError_t e = splat_enqueue(v, s->L.npos, dens[0], &s->cnt->cur[0], valid[0], s->nL, rho0, nullptr,
+    e = splat_enqueue(v, s->L.npos, dens[0], &s->cnt->cur[0], valid[0], s->nL, rho0, nullptr,
                                   point_sizes[0], img, w + 256, entries_cap(caps[0], v, point_sizes[0]), err, st);
     if (e == cudaSuccess)
         e = splat_enqueue(v, s->H.npos, dens[1], &s->cnt->cur[1], valid[1], s->capH, rho0, nullptr, point_sizes[1], img,
@@ -367,6 +368,7 @@ tss_status tss_solver_render(tss_solver* s, const tss_view* v, const float* poin
     if (e == cudaSuccess && s->nW > 0)
         e = splat_enqueue(v, s->wpos, nullptr, nw, nullptr, s->nW, rho0, black, point_sizes[2], img, w + 256,
                           entries_cap(caps[2], v, point_sizes[2]), err, st);
+    if (e == cudaSuccess) e = s->leave(st);
     if (e != cudaSuccess) return s->cuda_fail(e, "render");
     return TSS_OK;
 }

@@ -380,7 +380,7 @@ tss_status tss_server_run(tss_server* sv, int n, const tss_request* reqs, tss_re
         stats[i].arrival_s = reqs[i].arrival_s;
         stats[i].admit_s = stats[i].done_s = -1.0;
         stats[i].first_step = -1;
-        stats[i].status = TSS_TIMEOUT;  // not served (replaced below)
+        stats[i].status = TSS_CUDA_ERROR;  // not served: the run stopped before it (replaced below)
     }
     Run R{sv, n, reqs, stats, {}};
     // the GPU clock and the host clock start together

@@ -114,16 +114,20 @@ cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
     }
     if ((e = mark(3, s)) != cudaSuccess) return e;
     // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
-    launch_k_density_high(batched, launch.per_warp[0] != 0, gather_grid[0], launch.threads[0], s, P, V);
+    const bool fast = arith == TSS_ARITH_FAST;
+    auto gather = [&](int g) {
+        launch_gather(g, batched, launch.per_warp[g] != 0, fast, gather_grid[g], launch.threads[g], s, P, V);
+    };
+    gather(0);
     if ((e = mark(4, s)) != cudaSuccess) return e;
-    launch_k_density_low(batched, launch.per_warp[1] != 0, gather_grid[1], launch.threads[1], s, P, V);
+    gather(1);
     if ((e = mark(5, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
-    launch_k_force_low(batched, launch.per_warp[2] != 0, gather_grid[2], launch.threads[2], s, P, V);
+    gather(2);
     if ((e = mark(6, s)) != cudaSuccess) return e;
     launch_k_split(batched, std::min(split_ntiles, 8 * sm_count()), kSplitThreads, s, P, V);
     if ((e = mark(7, s)) != cudaSuccess) return e;
-    launch_k_force_high(batched, launch.per_warp[3] != 0, gather_grid[3], launch.threads[3], s, P, V);
+    gather(3);
     k_step_finish<<<1, 32, 0, s>>>(cnt);
     if ((e = mark(8, s)) != cudaSuccess) return e;
     return cudaGetLastError();
@@ -149,7 +153,7 @@ tss_status tss_solver::apply_launch(const tss_launch& l) {
         const long long cap = std::max(low ? nL : capH, 1) * lanes;
         const long long cover = (cap + t - 1) / t;
         if (l.persistent[g]) {
-            const int occ = gather_occupancy(g, batched, l.per_warp[g] != 0, t);
+            const int occ = gather_occupancy(g, batched, l.per_warp[g] != 0, arith == TSS_ARITH_FAST, t);
             if (occ <= 0) return fail(TSS_CUDA_ERROR, "occupancy query of a gather kernel failed");
             grid[g] = static_cast<int>(sms * occ);
         } else if (low && low_full) {
@@ -343,6 +347,20 @@ Params make_params(const SceneIn& sc) {
     recip_split(P.rh, P.inv_hi.y, P.inv_lo.y);
     P.nLs = sc.n_low;
     P.CHs = cfg->dims_high[0] * cfg->dims_high[1];
+    // FastArith's constants, from the same double values as the coefficients above
+    P.fTor = make_float2(static_cast<float>(2.0 / r), static_cast<float>(2.0 / rh));
+    P.fC = make_float2(static_cast<float>(10.0 / (14.0 * kPi * r * r)), static_cast<float>(10.0 / (14.0 * kPi * rh * rh)));
+    P.fG = make_float2(static_cast<float>(-60.0 / (14.0 * kPi * r * r * r)),
+                       static_cast<float>(-60.0 / (14.0 * kPi * rh * rh * rh)));
+    const double hs[3] = {r, 0.5 * (r + rh), rh};
+    float eps[3], kv[3];
+    for (int k = 0; k < 3; ++k) {
+        eps[k] = static_cast<float>(0.01 * hs[k] * hs[k]);
+        kv[k] = static_cast<float>(2.0 * hs[k] * cfg->alpha * static_cast<double>(cfg->speed_sound));
+    }
+    P.fEps = make_float3(eps[0], eps[1], eps[2]);
+    P.fKv = make_float3(kv[0], kv[1], kv[2]);
+    P.fKw = static_cast<float>(0.02 * static_cast<double>(cfg->speed_sound) * cfg->speed_sound);
     return P;
 }
 
@@ -366,7 +384,7 @@ const char* tss_status_string(tss_status st) {
         case TSS_CUDA_ERROR: return "CUDA error";
         case TSS_CAPACITY: return "particle pool capacity exceeded";
         case TSS_NUMERIC: return "NaN or Inf in the particle state";
-        case TSS_TIMEOUT: return "device-side wait timed out";
+        case TSS_GRID_INDEX: return "grid index check failed (inconsistent cell offsets)";
         case TSS_NO_DEVICE: return "no CUDA device";
     }
     return "unknown status";
@@ -560,6 +578,7 @@ tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
     if (!s || n_steps < 0) return TSS_INVALID_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default stream
     cudaError_t e;
+    if ((e = s->enter(st)) != cudaSuccess) return s->cuda_fail(e, "order step");
     while (n_steps > 0) {
         int b = 0;  // bucket: 1 << b steps
         if (!s->profile) b = n_steps >= 8 ? 3 : (n_steps >= 4 ? 2 : (n_steps >= 2 ? 1 : 0));
@@ -588,17 +607,18 @@ tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
         n_steps -= 1 << b;
     }
     s->uploaded[0] = s->uploaded[1] = false;
+    if ((e = s->leave(st)) != cudaSuccess) return s->cuda_fail(e, "record step");
     return TSS_OK;
 }
 
 tss_status tss_solver_sync(tss_solver* s) {
     if (!s) return TSS_INVALID_ARG;
-    cudaError_t e = cudaDeviceSynchronize();
+    cudaError_t e = s->wait_idle();
     if (e != cudaSuccess) return s->cuda_fail(e, "synchronize");
     Counters c;
-    if ((e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    if ((e = s->d2h(&c, s->cnt, sizeof(c))) != cudaSuccess)
         return s->cuda_fail(e, "read counters");
-    if (c.err & kErrTimeout) return s->fail(TSS_TIMEOUT, "a device-side look-back wait gave up");
+    if (c.err & kErrGridIndex) return s->fail(TSS_GRID_INDEX, "inconsistent grid offsets (an index check failed)");
     if (c.err & kErrCapacity) return s->fail(TSS_CAPACITY, "high-res pool capacity exceeded by a split");
     if (c.err & kErrNumeric) return s->fail(TSS_NUMERIC, "NaN/Inf density, pressure or acceleration");
     return TSS_OK;
@@ -606,10 +626,9 @@ tss_status tss_solver_sync(tss_solver* s) {
 
 tss_status tss_solver_counts(tss_solver* s, tss_counts* out) {
     if (!s || !out) return TSS_INVALID_ARG;
-    cudaError_t e = cudaStreamSynchronize(s->stream);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaError_t e = s->wait_idle();
     Counters c;
-    if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = s->d2h(&c, s->cnt, sizeof(c));
     if (e != cudaSuccess) return s->cuda_fail(e, "counts");
     out->n_low = c.cur[0];
     out->n_high = c.cur[1] - c.dropped;  // removed entries wait in the list for the next build
@@ -630,27 +649,27 @@ cudaError_t copy_list(tss_solver* s, int scale, int np, const tss_scale_state& o
     ScaleBufs& b = scale == 0 ? s->L : s->H;
     cudaError_t e = cudaSuccess;
     if (np == 0) return e;
-    if (o.id) e = cudaMemcpy(o.id, b.nid, sizeof(int32_t) * np, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && o.pos) e = cudaMemcpy(o.pos, b.npos, sizeof(float2) * np, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && o.vel) e = cudaMemcpy(o.vel, b.nvel, sizeof(float2) * np, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && o.state) e = cudaMemcpy(o.state, b.nst, np, cudaMemcpyDeviceToHost);
+    if (o.id) e = s->d2h(o.id, b.nid, sizeof(int32_t) * np);
+    if (e == cudaSuccess && o.pos) e = s->d2h(o.pos, b.npos, sizeof(float2) * np);
+    if (e == cudaSuccess && o.vel) e = s->d2h(o.vel, b.nvel, sizeof(float2) * np);
+    if (e == cudaSuccess && o.state) e = s->d2h(o.state, b.nst, np);
     if (e == cudaSuccess && (o.dens || o.pres)) {
         if (s->carry) {
-            if (o.dens) e = cudaMemcpy(o.dens, b.ndens, sizeof(float) * np, cudaMemcpyDeviceToHost);
-            if (e == cudaSuccess && o.pres) e = cudaMemcpy(o.pres, b.npres, sizeof(float) * np, cudaMemcpyDeviceToHost);
+            if (o.dens) e = s->d2h(o.dens, b.ndens, sizeof(float) * np);
+            if (e == cudaSuccess && o.pres) e = s->d2h(o.pres, b.npres, sizeof(float) * np);
         } else {
             // list order = last step's sorted order for the particles that existed then
             Counters cc;
-            e = cudaMemcpy(&cc, s->cnt, sizeof(cc), cudaMemcpyDeviceToHost);
+            e = s->d2h(&cc, s->cnt, sizeof(cc));
             int m = (cc.steps > 0 && !s->uploaded[scale]) ? cc.sorted[scale] : 0;
             if (m > np) m = np;
             if (o.dens) {
                 std::memset(o.dens, 0, sizeof(float) * np);
-                if (e == cudaSuccess && m) e = cudaMemcpy(o.dens, b.dens, sizeof(float) * m, cudaMemcpyDeviceToHost);
+                if (e == cudaSuccess && m) e = s->d2h(o.dens, b.dens, sizeof(float) * m);
             }
             if (o.pres) {
                 std::memset(o.pres, 0, sizeof(float) * np);
-                if (e == cudaSuccess && m) e = cudaMemcpy(o.pres, b.pres, sizeof(float) * m, cudaMemcpyDeviceToHost);
+                if (e == cudaSuccess && m) e = s->d2h(o.pres, b.pres, sizeof(float) * m);
             }
         }
     }
@@ -728,22 +747,22 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
         }
         seen[id] = 1;
     }
-    cudaError_t e = cudaDeviceSynchronize();
+    cudaError_t e = s->wait_idle();
     ScaleBufs& b = scale == 0 ? s->L : s->H;
     if (e == cudaSuccess && n > 0) {
-        e = cudaMemcpy(b.nid, in->id, sizeof(int32_t) * n, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(b.npos, in->pos, sizeof(float2) * n, cudaMemcpyHostToDevice);
+        e = s->h2d(b.nid, in->id, sizeof(int32_t) * n);
+        if (e == cudaSuccess) e = s->h2d(b.npos, in->pos, sizeof(float2) * n);
         if (e == cudaSuccess) {
-            if (in->vel) e = cudaMemcpy(b.nvel, in->vel, sizeof(float2) * n, cudaMemcpyHostToDevice);
-            else e = cudaMemset(b.nvel, 0, sizeof(float2) * n);
+            if (in->vel) e = s->h2d(b.nvel, in->vel, sizeof(float2) * n);
+            else e = s->memset0(b.nvel, sizeof(float2) * n);
         }
-        if (e == cudaSuccess) e = cudaMemcpy(b.nst, in->state, n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = s->h2d(b.nst, in->state, n);
         if (e == cudaSuccess && s->carry) {
-            if (in->dens) e = cudaMemcpy(b.ndens, in->dens, sizeof(float) * n, cudaMemcpyHostToDevice);
-            else e = cudaMemset(b.ndens, 0, sizeof(float) * n);
+            if (in->dens) e = s->h2d(b.ndens, in->dens, sizeof(float) * n);
+            else e = s->memset0(b.ndens, sizeof(float) * n);
             if (e == cudaSuccess) {
-                if (in->pres) e = cudaMemcpy(b.npres, in->pres, sizeof(float) * n, cudaMemcpyHostToDevice);
-                else e = cudaMemset(b.npres, 0, sizeof(float) * n);
+                if (in->pres) e = s->h2d(b.npres, in->pres, sizeof(float) * n);
+                else e = s->memset0(b.npres, sizeof(float) * n);
             }
         }
     }
@@ -753,7 +772,7 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
     }
     if (e == cudaSuccess) {
         Counters c;
-        e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+        e = s->d2h(&c, s->cnt, sizeof(c));
         if (e == cudaSuccess) {
             int nL = scale == 0 ? n : c.cur[0];
             int nH = scale == 1 ? n : c.cur[1];
@@ -771,10 +790,10 @@ tss_status tss_solver_upload(tss_solver* s, int scale, const tss_scale_state* in
 tss_status tss_solver_get_fresh(tss_solver* s, int* n, int32_t* parents) {
     if (!s || !n) return TSS_INVALID_ARG;
     Counters c;
-    cudaError_t e = cudaDeviceSynchronize();
-    if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+    cudaError_t e = s->wait_idle();
+    if (e == cudaSuccess) e = s->d2h(&c, s->cnt, sizeof(c));
     if (e == cudaSuccess && parents && c.n_fresh > 0)
-        e = cudaMemcpy(parents, s->split_ids, sizeof(int32_t) * c.n_fresh, cudaMemcpyDeviceToHost);
+        e = s->d2h(parents, s->split_ids, sizeof(int32_t) * c.n_fresh);
     if (e != cudaSuccess) return s->cuda_fail(e, "get fresh");
     *n = c.n_fresh;
     return TSS_OK;
@@ -784,8 +803,8 @@ tss_status tss_solver_set_fresh(tss_solver* s, int n, const int32_t* parents) {
     if (!s || n < 0 || n > s->nL || (n > 0 && !parents)) return TSS_INVALID_ARG;
     for (int i = 0; i < n; ++i)
         if (parents[i] < 0 || parents[i] >= s->slotsL) return s->fail(TSS_INVALID_ARG, "parent id out of range");
-    cudaError_t e = cudaDeviceSynchronize();
-    if (e == cudaSuccess && n > 0) e = cudaMemcpy(s->split_ids, parents, sizeof(int32_t) * n, cudaMemcpyHostToDevice);
+    cudaError_t e = s->wait_idle();
+    if (e == cudaSuccess && n > 0) e = s->h2d(s->split_ids, parents, sizeof(int32_t) * n);
     if (e == cudaSuccess) {
         k_set_fresh<<<1, 1, 0, s->stream>>>(s->cnt, n);
         e = cudaStreamSynchronize(s->stream);
@@ -797,8 +816,8 @@ tss_status tss_solver_set_fresh(tss_solver* s, int n, const int32_t* parents) {
 tss_status tss_solver_copy(tss_solver* s, int scale, int which, void* dst, size_t count, size_t* written) {
     if (!s || (scale != 0 && scale != 1)) return TSS_INVALID_ARG;
     Counters c;
-    cudaError_t e = cudaDeviceSynchronize();
-    if (e == cudaSuccess) e = cudaMemcpy(&c, s->cnt, sizeof(c), cudaMemcpyDeviceToHost);
+    cudaError_t e = s->wait_idle();
+    if (e == cudaSuccess) e = s->d2h(&c, s->cnt, sizeof(c));
     if (e != cudaSuccess) return s->cuda_fail(e, "copy");
     ScaleBufs& b = scale == 0 ? s->L : s->H;
     // particles sorted in the last step: the count before its splits
@@ -826,7 +845,7 @@ tss_status tss_solver_copy(tss_solver* s, int scale, int which, void* dst, size_
     if (written) *written = n;
     if (!dst) return TSS_OK;
     if (count < n) return s->fail(TSS_INVALID_ARG, "destination too small");
-    if (n && (e = cudaMemcpy(dst, src, n * esz, cudaMemcpyDeviceToHost)) != cudaSuccess) return s->cuda_fail(e, "copy");
+    if (n && (e = s->d2h(dst, src, n * esz)) != cudaSuccess) return s->cuda_fail(e, "copy");
     return TSS_OK;
 }
 
@@ -848,7 +867,7 @@ tss_status tss_solver_profile(tss_solver* s, int enable) {
     if (!s) return TSS_INVALID_ARG;
     const bool want = enable != 0;
     if (want == s->profile) return TSS_OK;
-    cudaError_t e = cudaDeviceSynchronize();
+    cudaError_t e = s->wait_idle();
     if (e != cudaSuccess) return s->cuda_fail(e, "profile");
     if (want)
         for (auto& x : s->ev)
@@ -861,7 +880,7 @@ tss_status tss_solver_profile(tss_solver* s, int enable) {
 tss_status tss_solver_stage_times(tss_solver* s, float* ms, int n) {
     if (!s || !ms || n < TSS_NUM_STAGES) return TSS_INVALID_ARG;
     if (!s->profile) return s->fail(TSS_INVALID_ARG, "profiling is off");
-    cudaError_t e = cudaDeviceSynchronize();
+    cudaError_t e = s->wait_idle();
     for (int k = 0; k < TSS_NUM_STAGES && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&ms[k], s->ev[k], s->ev[k + 1]);
     if (e != cudaSuccess) return s->cuda_fail(e, "stage times");
     return TSS_OK;
@@ -895,10 +914,15 @@ tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low
     void* dev[3];
     const tss_status st = read_targets(s, host_low, cap_low, host_high, cap_high, counts, dev);
     if (st != TSS_OK) return st;
-    k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        s->L.npos, s->H.npos, &s->cnt->cur[0], static_cast<float2*>(dev[0]), cap_low, static_cast<float2*>(dev[1]),
-        cap_high, static_cast<int*>(dev[2]));
-    const cudaError_t e = cudaGetLastError();
+    const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    cudaError_t e = s->enter(cs);
+    if (e == cudaSuccess) {
+        k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, cs>>>(
+            s->L.npos, s->H.npos, &s->cnt->cur[0], static_cast<float2*>(dev[0]), cap_low,
+            static_cast<float2*>(dev[1]), cap_high, static_cast<int*>(dev[2]));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = s->leave(cs);
     return e == cudaSuccess ? TSS_OK : s->cuda_fail(e, "read_positions");
 }
 
@@ -945,13 +969,15 @@ tss_status tss_solver_read_positions_async(tss_solver* s, float* host_low, int c
     const int b = static_cast<int>(rb.issued & 1);
     const cudaStream_t cs = static_cast<cudaStream_t>(stream);
     // the buffer's previous host copy (two calls ago) must be done before it is refilled
-    if (rb.issued >= 2) e = cudaStreamWaitEvent(cs, rb.done[b], 0);
+    e = s->enter(cs);
+    if (e == cudaSuccess && rb.issued >= 2) e = cudaStreamWaitEvent(cs, rb.done[b], 0);
     if (e == cudaSuccess) {
         k_read_positions<<<read_blocks(std::max(cap_low, cap_high)), 256, 0, cs>>>(
             s->L.npos, s->H.npos, &s->cnt->cur[0], rb.low[b], cap_low, rb.high[b], cap_high, rb.counts[b]);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaEventRecord(rb.staged[b], cs);
+    if (e == cudaSuccess) e = s->leave(cs);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(rb.stream, rb.staged[b], 0);
     // A single scene's low-res list always holds all nL particles, so its length is
     // known here and a copy engine moves it, leaving the SMs to the next step; the
@@ -991,9 +1017,25 @@ tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out) {
 tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in) {
     if (!s || !in) return TSS_INVALID_ARG;
     // steps run on callers' streams: wait for all of them before the old graphs go
-    cudaError_t e = cudaDeviceSynchronize();
+    cudaError_t e = s->wait_idle();
     if (e != cudaSuccess) return s->cuda_fail(e, "set launch");
     return s->apply_launch(*in);
+}
+
+tss_status tss_solver_set_arith(tss_solver* s, int mode) {
+    if (!s || (mode != TSS_ARITH_EXACT && mode != TSS_ARITH_FAST)) return TSS_INVALID_ARG;
+    if (mode == s->arith) return TSS_OK;
+    // the old graphs may still run on callers' streams
+    cudaError_t e = s->wait_idle();
+    if (e != cudaSuccess) return s->cuda_fail(e, "set arith");
+    s->arith = mode;
+    return s->apply_launch(s->launch);  // grids of persistent shapes follow the kernels' occupancy
+}
+
+tss_status tss_solver_get_arith(tss_solver* s, int* mode) {
+    if (!s || !mode) return TSS_INVALID_ARG;
+    *mode = s->arith;
+    return TSS_OK;
 }
 
 // Stage of each gather in the profiled step (tss_solver_stage_times).

@@ -118,6 +118,7 @@ struct tss_solver {
     int blocksL = 1, blocksH = 1;           // the non-gather particle kernels
     bool low_full = true;                   // the low-res list is always full (single scenes, batches)
     tss_launch launch{};                    // the gathers' launch shape
+    int arith = TSS_ARITH_EXACT;            // the gathers' arithmetic (tss_solver_set_arith)
     int gather_grid[TSS_NUM_GATHERS] = {};  // blocks of each gather for that shape
     bool uploaded[2] = {false, false};  // state replaced since the last step
     bool profile = false;
@@ -166,6 +167,52 @@ struct tss_solver {
         int cap_low = 0, cap_high = 0;  // entries each staging buffer holds per list
     } rb;
 
+    // Ordering of the handle's work on callers' streams.  Every call that enqueues
+    // work on a caller's stream first makes that stream wait for the handle's last
+    // such work when it went to another stream (enter), and afterwards records
+    // work_ev there (leave).  wait_idle() then waits for this handle's work only --
+    // that event and the handle's own streams -- instead of the whole device, so
+    // other solvers and the host application's streams keep running.  Streams under
+    // capture are left as they are (a record there would not be a real event).
+    cudaEvent_t work_ev = nullptr;
+    cudaStream_t work_stream = nullptr;
+    bool work_pending = false;
+
+    static bool capturing(cudaStream_t cs) {
+        cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+        return cudaStreamIsCapturing(cs, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+    }
+    cudaError_t enter(cudaStream_t cs) {
+        if (!work_pending || cs == work_stream || capturing(cs)) return cudaSuccess;
+        return cudaStreamWaitEvent(cs, work_ev, 0);
+    }
+    cudaError_t leave(cudaStream_t cs) {
+        if (capturing(cs)) return cudaSuccess;
+        cudaError_t e = cudaSuccess;
+        if (!work_ev && (e = cudaEventCreateWithFlags(&work_ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(work_ev, cs)) != cudaSuccess) return e;
+        work_stream = cs;
+        work_pending = true;
+        return cudaSuccess;
+    }
+    cudaError_t wait_idle() {
+        cudaError_t e = cudaSuccess;
+        if (work_pending) e = cudaEventSynchronize(work_ev);
+        if (e == cudaSuccess && stream) e = cudaStreamSynchronize(stream);
+        if (e == cudaSuccess && rb.stream) e = cudaStreamSynchronize(rb.stream);
+        return e;
+    }
+    // Copies and clears on the handle's own stream; the copies return when done.
+    cudaError_t d2h(void* dst, const void* src, size_t bytes) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream);
+        return e == cudaSuccess ? cudaStreamSynchronize(stream) : e;
+    }
+    cudaError_t h2d(void* dst, const void* src, size_t bytes) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+        return e == cudaSuccess ? cudaStreamSynchronize(stream) : e;
+    }
+    cudaError_t memset0(void* dst, size_t bytes) { return cudaMemsetAsync(dst, 0, bytes, stream); }
+
     tss_status fail(tss_status st, const std::string& msg) {
         err = msg;
         return st;
@@ -192,7 +239,9 @@ struct tss_solver {
     }
 
     ~tss_solver() {
+        wait_idle();
         drop_graph();
+        if (work_ev) cudaEventDestroy(work_ev);
         for (auto& x : ev)
             if (x) cudaEventDestroy(x);
         if (stream) cudaStreamDestroy(stream);

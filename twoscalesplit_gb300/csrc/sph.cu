@@ -1,372 +1,9 @@
-// sph.cu -- density, force, split and relaxation kernels of the two-scale step.
-//
-// Particles are in (cell, id) order.  Because the arrays are sorted by cell, the
-// candidates of one row of the 3x3 (or wider cross-scale) cell window are one
-// contiguous span [off[row + cx0], off[row + cx1 + 1]).  Each particle's sums take
-// its candidates in the reference's order (cells row by row, particles in cell
-// order), which keeps every FP32 sum identical to the reference's for the same
-// list order.  The gathers walk a particle's window one of two ways (gather.cuh):
-// one particle per thread, consecutive threads walking overlapping spans so that
-// neighbour loads are shared through L1 (the throughput form), or one particle per
-// warp with the candidates spread over the lanes (for scenes too small to fill the
-// GPU); both give the same bits.
-//
-// Each kernel's per-particle work is an inlined function of the particle's Params:
-// the kernel's own constants for a single scene, the scene's table row for a
-// batch.  The row is read through a reference, so each field is loaded where it is
-// used: a copy of the whole row kept every field live in registers across the
-// neighbour loops, and the batched gathers spilled and ran 5 % slower.  A scene's
-// cell windows index its grid at its cell base in the global cell space, so one
-// sort and one offset table serve all scenes of a batch.
-#include "gather.cuh"
-#include "sph.cuh"
+// sph.cu -- the step's kernels other than the gathers (split compaction and
+// children, relaxation, step finish), the gathers in the reference's arithmetic
+// (gathers.cuh with ExactArith), and the launchers that pick the arithmetic.
+#include "gathers.cuh"
 
 namespace tss {
-
-namespace {
-__device__ __forceinline__ int nthreads() { return gridDim.x * blockDim.x; }
-__device__ __forceinline__ int tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ float2 sub(float2 a, float2 b) { return sub2(a, b); }
-__device__ __forceinline__ void add_density(float& d, float t) { d += t; }
-
-// The particles of a gather, one per thread (G = PerThread) or one per warp
-// (G = PerWarp, every lane of the warp taking the same particle).
-template <class G, class F>
-__device__ __forceinline__ void for_each_particle(int n, F&& f) {
-    if constexpr (G::kWarp) {
-        const int nw = nthreads() >> 5;
-        for (int i = tid() >> 5; i < n; i += nw) f(i);
-    } else {
-        for (int i = tid(); i < n; i += nthreads()) f(i);
-    }
-}
-}  // namespace
-
-
-// ---------------------------------------------------------------------------
-// High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
-// ---------------------------------------------------------------------------
-template <class G>
-__device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i) {
-    const ScaleView& H = V.H;
-    const ScaleView& L = V.L;
-    const int* offH = H.off + P.cbH;
-    const int* offL = L.off + P.cbL;
-    const float2 p = H.pos[i];
-    const unsigned s = H.st[i];
-    float d = 0.0f, dl = 0.0f;
-    float x = 0.0f;
-    const auto term = [&](int) { return pair_density(P, sqrtf(x)); };
-    int csx, csy, cex, cey;
-    grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
-    grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
-    G::window(
-        offH, P.dimH[0], csx, cex, csy, cey,
-        [&](int k) {
-            if (!lamHH(s, H.st[k])) return false;
-            x = sq(sub(p, H.pos[k]));
-            return x <= P.Tle_rh;
-        },
-        term, add_density, d);
-    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
-    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    if (P.q1) {
-        // The reference reads the HIGH sorted list at LOW-grid ranges of its own
-        // scene; past the scene's n_high that list still holds its initial identity
-        // (slot t at position t).  A row's range [a, b) of low-list positions t
-        // (t - baseL >= 0: offsets only grow) is taken in two runs, in order: the
-        // positions below baseL + n_high, which are the high-list entries
-        // t - baseL + baseH, and the rest, through the slot map.
-        const int baseL = offL[0], baseH = offH[0];
-        const int nHs = offH[P.CHs] - baseH;
-        const int tH = baseL + nHs;   // first position past the scene's high-res list
-        const int dH = baseH - baseL;  // low-list position -> high-list entry
-        for (int cy = csy; cy <= cey; ++cy) {
-            const int row = cy * P.dimL[0];
-            const int a = offL[row + csx], b = offL[row + cex + 1];
-            const int m = min(b, max(a, tH));
-            G::span(
-                a + dH, m + dH,
-                [&](int k) {
-                    if (!lamHL(s, H.st[k])) return false;
-                    x = sq(sub(p, H.pos[k]));
-                    return x <= P.Tle_rh;
-                },
-                term, add_density, d);
-            G::span(
-                m, b,
-                [&](int t) {
-                    const int tl = t - baseL;
-                    const int slot = 4 * P.sbL + tl;
-                    const int k = (tl < 4 * P.nLs && slot < P.slotsH) ? H.map[slot] : -1;
-                    float2 pj = make_float2(0.0f, 0.0f);
-                    unsigned sj = 0;
-                    if (k >= 0) {
-                        pj = H.pos[k];
-                        sj = H.st[k];
-                    }
-                    if (!lamHL(s, sj)) return false;
-                    x = sq(sub(p, pj));
-                    return x <= P.Tle_rh;
-                },
-                term, add_density, d);
-        }
-    } else {
-        G::window(
-            offL, P.dimL[0], csx, cex, csy, cey,
-            [&](int k) {
-                if (!lamHL(s, L.st[k])) return false;
-                x = sq(sub(p, L.pos[k]));
-                return x <= P.Tle_rh;
-            },
-            term, add_density, dl);
-    }
-    d *= P.mH;
-    dl *= P.mL;
-    d += dl;
-    const float pr = tait(d, P);
-    if (G::leader()) {
-        H.dens[i] = d;
-        H.pres[i] = pr;
-        H.q[i] = pr / (d * d);
-        if (!isfinite(d) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
-    }
-}
-
-template <bool B, class G>
-__global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
-    for_each_particle<G>(V.cnt->cur[1], [&](int i) {
-        if constexpr (B) {
-            const Params& P = V.table[V.scH[i]];
-            density_high_one<G>(P, V, i);
-        } else {
-            density_high_one<G>(P0, V, i);
-        }
-    });
-}
-
-// ---------------------------------------------------------------------------
-// Low-res density + Tait, computeParticleDensityPressure (WCSPHSolver.cu:1342-1424)
-// ---------------------------------------------------------------------------
-template <class G>
-__device__ __forceinline__ void density_low_one(const Params& P, const StepView& V, int i, bool cross) {
-    const ScaleView& H = V.H;
-    const ScaleView& L = V.L;
-    const float2 p = L.pos[i];
-    const unsigned s = L.st[i];
-    float d = 0.0f, dh = 0.0f;
-    float x = 0.0f;
-    const auto term = [&](int) { return pair_density(P, sqrtf(x)); };
-    int csx, csy, cex, cey;
-    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
-    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    G::window(
-        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
-        [&](int k) {
-            x = sq(sub(p, L.pos[k]));
-            return x <= P.Tle_r;
-        },
-        term, add_density, d);
-    if (cross) {  // only state-0 high-res particles can contribute (lambda_LH)
-        grid_coord_s<1>(P, p.x, p.y, -P.r, csx, csy);
-        grid_coord_s<1>(P, p.x, p.y, P.r, cex, cey);
-        G::window(
-            H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
-            [&](int k) {
-                if (!lamLH(s, H.st[k])) return false;
-                x = sq(sub(p, H.pos[k]));
-                return x <= P.Tle_r;
-            },
-            term, add_density, dh);
-    }
-    d *= P.mL;
-    dh *= P.mH;
-    const float rho = d + dh;
-    const float pr = tait(rho, P);
-    if (G::leader()) {
-        L.dens[i] = rho;
-        L.pres[i] = pr;
-        L.q[i] = pr / (rho * rho);
-        if (!isfinite(rho) || !isfinite(pr)) atomicOr(&V.cnt->err, kErrNumeric);
-    }
-}
-
-template <bool B, class G>
-__global__ void __launch_bounds__(256) k_density_low(Params P0, StepView V) {
-    const bool cross = V.cnt->h_state0 != 0;
-    for_each_particle<G>(V.cnt->cur[0], [&](int i) {
-        if constexpr (B) {
-            const Params& P = V.table[V.scL[i]];
-            density_low_one<G>(P, V, i, cross);
-        } else {
-            density_low_one<G>(P0, V, i, cross);
-        }
-    });
-}
-
-// Wall term of a force sum (updateAccCell 562-579 / updateAccCellComplementHigh
-// 867-884): every wall particle of the window's cells, in cell order.  Pairs with
-// sqrtf(x) > rad have q >= 2 and add exactly zero, so they are skipped.  q = 2d/rad
-// through rad's reciprocal split (yh, yl), as in the pair kernels.
-template <class G>
-__device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, float2 p, int csx, int cex, int csy,
-                                           int cey, float rad, float yh, float yl, float Tle, float cB) {
-    float2 accB = make_float2(0.f, 0.f);
-    const int* woff = V.woff + P.cbL;
-    const float2* wpos = V.wpos + P.wb;
-    float2 pik = make_float2(0.f, 0.f);
-    float x = 0.0f;
-    for (int cy = csy; cy <= cey; ++cy) {
-        const int row = cy * P.dimL[0];
-        G::span(
-            woff[row + csx], woff[row + cex + 1],
-            [&](int k) {
-                pik = sub(p, wpos[k]);
-                x = sq(pik);
-                return !(x > Tle);  // NaN passes: the reference's 0 * NaN offset propagates it
-            },
-            [&](int) {
-                const float d = sqrtf(x);
-                const float gm = wall_weight_q(d, div_const(d * 2.0f, rad, yh, yl), P.cs);
-                return make_float2(cB * gm * pik.x, cB * gm * pik.y);
-            },
-            [](float2& a, float2 t) {
-                a.x += t.x;
-                a.y += t.y;
-            },
-            accB);
-    }
-    return accB;
-}
-
-// ---------------------------------------------------------------------------
-// Low-res force + advance + split test: computeParticleAcceleration
-// (WCSPHSolver.cu:1648-1865) with advance (1604-1646) fused; its predicted position
-// is the advanced position bit for bit.  The fluid and wall sums are independent
-// accumulators, so they are taken in two passes over the window.  The new position
-// also gives the entry's key for the next step's grid.  Returns the split flag.
-// ---------------------------------------------------------------------------
-template <class G>
-__device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V, int i, bool cross) {
-    const ScaleView& H = V.H;
-    const ScaleView& L = V.L;
-    float2 p = L.pos[i], v = L.vel[i];
-    const unsigned s = L.st[i];
-    const float dens = L.dens[i], qi = L.q[i];
-    PairTerms fl{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // (acc, accT)
-    float2 pij = make_float2(0.f, 0.f);
-    float x = 0.0f;
-    int csx, csy, cex, cey;
-    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
-    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    G::window(
-        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
-        [&](int k) {
-            pij = sub(p, L.pos[k]);
-            x = sq(pij);
-            return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
-        },
-        [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.r); },
-        add_terms, fl);
-    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.r, P.inv_hi.x, P.inv_lo.x, P.Tle_r, P.cBL);
-    PairTerms fh{make_float2(0.f, 0.f), fl.t};  // (accH, accT): the sigma sum continues
-    if (cross) {
-        grid_coord_s<1>(P, p.x, p.y, -P.r, csx, csy);
-        grid_coord_s<1>(P, p.x, p.y, P.r, cex, cey);
-        G::window(
-            H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
-            [&](int k) {
-                if (!lamLH(s, H.st[k])) return false;
-                pij = sub(p, H.pos[k]);
-                x = sq(pij);
-                return x != 0.0f && x <= P.Tlt_r;
-            },
-            [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.hx); },
-            add_terms, fh);
-    }
-    float2 acc = fl.a, accH = fh.a;
-    const float2 accT = fh.t;
-    acc.x *= -P.mL;
-    acc.y *= -P.mL;
-    accH.x *= -P.mH;
-    accH.y *= -P.mH;
-    acc.x += accH.x;
-    acc.y += accH.y;
-    acc.x -= P.sigma * accT.x;
-    acc.y -= P.sigma * accT.y;
-    acc.x += accB.x;
-    acc.y += accB.y;
-    acc.y -= P.g;
-    v.x += P.dt * acc.x;
-    v.y += P.dt * acc.y;
-    p.x += P.dt * v.x;
-    p.y += P.dt * v.y;
-    // split test on the predicted position (computeParticleAcceleration 1810-1835)
-    // against the ROI of this step; with TSS_FLAG_MERGE a split parent outside it
-    // merges back
-    const float kf = static_cast<float>(V.cnt->steps - P.step0);
-    const float rx0 = P.roi[0] + kf * P.roi_vdt[0], rx1 = P.roi[2] + kf * P.roi_vdt[0];
-    const float ry0 = P.roi[1] + kf * P.roi_vdt[1], ry1 = P.roi[3] + kf * P.roi_vdt[1];
-    const bool in_roi = rx0 < p.x && p.x < rx1 && ry0 < p.y && p.y < ry1;
-    bool flag = false;
-    uint8_t ns = static_cast<uint8_t>(s);
-    if (s == 0u && in_roi) {
-        ns = 1;
-        flag = true;
-    } else if (P.merge && s == 1u && !in_roi) {
-        ns = 0;
-    }
-    if (G::leader()) {
-        L.acc[i] = acc;
-        if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
-        L.npos[i] = p;
-        L.nvel[i] = v;
-        L.nid[i] = L.id[i];
-        grid_key(L.gcount, L.gkey, L.grank, L.gtile, i,
-                 P.cbL + cell_hash_s<0>(P, p));
-        L.nst[i] = ns;
-        V.split_flag[i] = flag ? 1 : 0;
-        if (L.ndens) {
-            L.ndens[i] = dens;
-            L.npres[i] = L.pres[i];
-        }
-    }
-    return flag;
-}
-
-// One particle per thread: a warp-uniform loop (every lane makes the same number of
-// trips, lanes past n inactive) so the ballot that feeds the split compaction sees
-// whole warps; a warp's 32 particles lie in one compaction tile (kSplitTile % 32 ==
-// 0).  One particle per warp: the leader counts its particle's split.
-// 48 registers (five blocks per SM) in both forms.  The batched form measured the
-// same at 40 and 48 on a batch of 512 mixed scenes (4.11 / 4.08 ms), 3-7 % faster
-// at 48 on batches of one scene, and 10 % slower at 64.
-template <bool B, class G>
-__global__ void __launch_bounds__(256, 5) k_force_low(Params P0, StepView V) {
-    const int n = V.cnt->cur[0];
-    const bool cross = V.cnt->h_state0 != 0;
-    const auto one = [&](int i) {
-        if constexpr (B) {
-            const Params& P = V.table[V.scL[i]];
-            return force_low_one<G>(P, V, i, cross);
-        } else {
-            return force_low_one<G>(P0, V, i, cross);
-        }
-    };
-    if constexpr (G::kWarp) {
-        for_each_particle<G>(n, [&](int i) {
-            if (one(i) && G::leader()) atomicAdd(&V.split_tile[i / kSplitTile], 1u);
-        });
-    } else {
-        const int lane = threadIdx.x & 31;
-        for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-            const int i = base + threadIdx.x;
-            const bool flag = i < n && one(i);
-            const unsigned m = __ballot_sync(0xffffffffu, flag);
-            if (lane == 0 && m) atomicAdd(&V.split_tile[(base + (threadIdx.x & ~31)) / kSplitTile], __popc(m));
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Ordered stream compaction of the split flags (warp ballots + block scan; the
@@ -484,127 +121,6 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(Params P0, StepView V) 
         }
         __syncthreads();  // s_warp / s_red are reused by the next tile
     }
-}
-
-// ---------------------------------------------------------------------------
-// High-res force + integrate + tether: computeParticleAccelerationAndAdvanceHigh
-// (WCSPHSolver.cu:1867-2033) and adjustOrInjectTransientHighD (1097-1172).
-// Reads see the pre-step state (the reference integrates in place, a data race);
-// low-res states are read after this step's split marks, as in the reference.
-// ---------------------------------------------------------------------------
-template <class G>
-__device__ __forceinline__ void force_high_one(const Params& P, const StepView& V, int i) {
-    const ScaleView& H = V.H;
-    const ScaleView& L = V.L;
-    float2 p = H.pos[i], v = H.vel[i];
-    const unsigned s = H.st[i];
-    const float dens = H.dens[i], qi = H.q[i];
-    PairTerms fh{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // (acc, accT)
-    float2 pij = make_float2(0.f, 0.f);
-    float x = 0.0f;
-    int csx, csy, cex, cey;
-    grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
-    grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
-    G::window(
-        H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
-        [&](int k) {
-            if (!lamHH(s, H.st[k])) return false;
-            pij = sub(p, H.pos[k]);
-            x = sq(pij);
-            return x != 0.0f && x <= P.Tlt_rh;
-        },
-        [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j], P.rh); },
-        add_terms, fh);
-    grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
-    grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    PairTerms fl{make_float2(0.f, 0.f), fh.t};  // (accL, accT): the sigma sum continues
-    G::window(
-        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
-        [&](int k) {
-            const unsigned sj = L.nst[k];  // low-res states after this step's split marks
-            if (!(lamHL(s, sj) && notDeleted(sj))) return false;
-            pij = sub(p, L.pos[k]);
-            x = sq(pij);
-            return x != 0.0f && x <= P.Tlt_r;
-        },
-        [&](int j) { return pair_terms(P, pij, sqrtf(x), sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j], P.hx); },
-        add_terms, fl);
-    const float2 accB = wall_sum<G>(P, V, p, csx, cex, csy, cey, P.rh, P.inv_hi.y, P.inv_lo.y, P.Tle_rh, P.cBH);
-    float2 acc = fh.a, accL = fl.a;
-    const float2 accT = fl.t;
-    acc.x *= -P.mH;
-    acc.y *= -P.mH;
-    accL.x *= -P.mL;
-    accL.y *= -P.mL;
-    acc.x -= P.sigma * accT.x;
-    acc.y -= P.sigma * accT.y;
-    acc.x += accL.x;
-    acc.y += accL.y;
-    acc.x += accB.x;
-    acc.y += accB.y;
-    acc.y -= P.g;
-    v.x += P.dt * acc.x;
-    v.y += P.dt * acc.y;
-    p.x += P.dt * v.x;
-    p.y += P.dt * v.y;
-    // tether to the parent after the parent's advance (adjustPosition, 1007-1022);
-    // with TSS_FLAG_MERGE the children of a parent that merged back in this step
-    // are removed instead
-    const int id = H.id[i];
-    const int parent = id >> 2;
-    bool drop = false;
-    if (parent >= 0 && parent < P.slotsL) {
-        const int pi = L.map[parent];
-        drop = P.merge && pi >= 0 && L.st[pi] == 1 && L.nst[pi] == 0;
-        if (pi >= 0 && L.st[pi] == 1 && !drop) {
-            const float2 pl = L.npos[pi];
-            const float rho = L.dens[pi];
-            const float2 pji = sub(p, pl);
-            const float dist = vnorm(pji);
-            const float lim = static_cast<float>(fmin(
-                static_cast<double>(dist), 0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(rho) * kPi))));
-            if (!(P.tether_guard && dist == 0.0f)) {  // guarded: a child on its parent stays there
-                p.x = pl.x + lim / dist * pji.x;
-                p.y = pl.y + lim / dist * pji.y;
-            }
-        }
-    }
-    if (!G::leader()) return;
-    H.acc[i] = acc;
-    if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
-    H.npos[i] = p;
-    H.nvel[i] = v;
-    H.nst[i] = static_cast<uint8_t>(drop ? 2u : s);
-    H.nid[i] = id;
-    if (drop) {  // out of the next grid build, and of the slot map
-        H.gkey[i] = -1;
-        H.map[id] = -1;
-        atomicAdd(&V.cnt->n_drop, 1);
-    } else {
-        grid_key(H.gcount, H.gkey, H.grank, H.gtile, i, P.cbH + cell_hash_s<1>(P, p));
-    }
-    if (H.ndens) {
-        H.ndens[i] = dens;
-        H.npres[i] = H.pres[i];
-    }
-}
-
-// Register budgets measured per form.  The batched form reads each particle's
-// parameters from the scene table: at 40 registers it spilled ~300 bytes, at 48 a
-// third of that, at 64 (four blocks per SM) nothing -- as fast as 48 on a batch of
-// 512 mixed scenes and 15 % faster on a batch of one 162k-particle scene.  The
-// single-scene form at 48 registers (five blocks) spills 64 bytes instead of 120
-// at 40 and measured 3-4 % faster.
-template <bool B, class G>
-__global__ void __launch_bounds__(256, B ? 4 : 5) k_force_high(Params P0, StepView V) {
-    for_each_particle<G>(V.cnt->cur[1], [&](int i) {
-        if constexpr (B) {
-            const Params& P = V.table[V.scH[i]];
-            force_high_one<G>(P, V, i);
-        } else {
-            force_high_one<G>(P0, V, i);
-        }
-    });
 }
 
 // ---------------------------------------------------------------------------
@@ -777,29 +293,24 @@ __global__ void k_step_finish(Counters* c) {
     }
 }
 
-// Host-side launchers (the templates stay in this translation unit).  A gather's
-// launcher selects the batched form (B) and the walk (one particle per thread or
-// per warp).
-#define TSS_GATHER_LAUNCHER(NAME)                                                                   \
-    void launch_##NAME(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P, \
-                       const StepView& V) {                                                          \
-        if (batched) {                                                                               \
-            if (warp)                                                                                \
-                NAME<true, PerWarp><<<blocks, threads, 0, s>>>(P, V);                                \
-            else                                                                                     \
-                NAME<true, PerThread><<<blocks, threads, 0, s>>>(P, V);                              \
-        } else {                                                                                     \
-            if (warp)                                                                                \
-                NAME<false, PerWarp><<<blocks, threads, 0, s>>>(P, V);                               \
-            else                                                                                     \
-                NAME<false, PerThread><<<blocks, threads, 0, s>>>(P, V);                             \
-        }                                                                                            \
-    }
-TSS_GATHER_LAUNCHER(k_density_high)
-TSS_GATHER_LAUNCHER(k_density_low)
-TSS_GATHER_LAUNCHER(k_force_low)
-TSS_GATHER_LAUNCHER(k_force_high)
-#undef TSS_GATHER_LAUNCHER
+// Host-side launchers.  The gathers come in two arithmetics: ExactArith here,
+// FastArith in sph_fast.cu (launch_gather_fast, gather_occupancy_fast).
+void launch_gather_fast(int g, bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
+                        const StepView& V);
+int gather_occupancy_fast(int g, bool batched, bool warp, int threads);
+
+void launch_gather(int g, bool batched, bool warp, bool fast, int blocks, int threads, cudaStream_t s,
+                   const Params& P, const StepView& V) {
+    if (fast)
+        launch_gather_fast(g, batched, warp, blocks, threads, s, P, V);
+    else
+        launch_gather_a<ExactArith>(g, batched, warp, blocks, threads, s, P, V);
+}
+
+int gather_occupancy(int g, bool batched, bool warp, bool fast, int threads) {
+    return fast ? gather_occupancy_fast(g, batched, warp, threads)
+                : gather_occupancy_a<ExactArith>(g, batched, warp, threads);
+}
 
 #define TSS_LAUNCHER(NAME)                                                                        \
     void launch_##NAME(bool batched, int blocks, int threads, cudaStream_t s, const Params& P,   \
@@ -813,37 +324,5 @@ TSS_LAUNCHER(k_split)
 TSS_LAUNCHER(k_relax_density)
 TSS_LAUNCHER(k_relax_force)
 #undef TSS_LAUNCHER
-
-namespace {
-template <class K>
-int occupancy(K kernel, int threads) {
-    int n = 0;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) == cudaSuccess ? n : 0;
-}
-
-template <bool B, class G>
-int gather_occupancy_of(int g, int threads) {
-    switch (g) {
-        case 0:
-            return occupancy(k_density_high<B, G>, threads);
-        case 1:
-            return occupancy(k_density_low<B, G>, threads);
-        case 2:
-            return occupancy(k_force_low<B, G>, threads);
-        case 3:
-            return occupancy(k_force_high<B, G>, threads);
-        default:
-            return 0;
-    }
-}
-}  // namespace
-
-// Resident blocks per SM of gather g (0 high-res density, 1 low-res density,
-// 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error.
-int gather_occupancy(int g, bool batched, bool warp, int threads) {
-    if (batched)
-        return warp ? gather_occupancy_of<true, PerWarp>(g, threads) : gather_occupancy_of<true, PerThread>(g, threads);
-    return warp ? gather_occupancy_of<false, PerWarp>(g, threads) : gather_occupancy_of<false, PerThread>(g, threads);
-}
 
 }  // namespace tss

@@ -64,20 +64,15 @@ template <bool B> __global__ void k_relax_force(Params P0, StepView V);
 __global__ void k_relax_apply(Params P0, StepView V);
 __global__ void k_step_finish(Counters* c);
 
-// host launchers (batched selects B; warp: one particle per warp instead of per thread)
-void launch_k_density_high(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
-                           const StepView& V);
-void launch_k_density_low(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
-                          const StepView& V);
-void launch_k_force_low(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
-                        const StepView& V);
-void launch_k_force_high(bool batched, bool warp, int blocks, int threads, cudaStream_t s, const Params& P,
-                         const StepView& V);
+// host launchers (batched selects B; warp: one particle per warp instead of per
+// thread; fast: FastArith instead of ExactArith, arith.cuh).  Gather g: 0 high-res
+// density, 1 low-res density, 2 low-res force, 3 high-res force.
+void launch_gather(int g, bool batched, bool warp, bool fast, int blocks, int threads, cudaStream_t s,
+                   const Params& P, const StepView& V);
 void launch_k_split(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 void launch_k_relax_density(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 void launch_k_relax_force(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
-// resident blocks per SM of gather g (0 high-res density, 1 low-res density,
-// 2 low-res force, 3 high-res force) at `threads` threads per block; 0 on error
-int gather_occupancy(int g, bool batched, bool warp, int threads);
+// resident blocks per SM of gather g at `threads` threads per block; 0 on error
+int gather_occupancy(int g, bool batched, bool warp, bool fast, int threads);
 
 }  // namespace tss

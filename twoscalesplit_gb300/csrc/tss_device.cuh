@@ -15,7 +15,7 @@ constexpr double kPi = 3.14159265358979323846;  // WCSPHSolver.cu:19
 // error word bits (mirror TSS_ERR_* in include/tss.h)
 constexpr unsigned kErrCapacity = 0x1u;
 constexpr unsigned kErrNumeric = 0x2u;
-constexpr unsigned kErrTimeout = 0x4u;  // inconsistent grid offsets (no device-side wait exists)
+constexpr unsigned kErrGridIndex = 0x4u;  // a grid index check failed: inconsistent cell offsets
 
 struct Params {
     float ox, oy;
@@ -46,6 +46,13 @@ struct Params {
     float Tle_r, Tlt_r, Tle_rh, Tlt_rh;
     // reciprocal splits of (r, rh) for div_const: hi = RN(1/r_s), lo = RN(1/r_s - hi)
     float2 inv_hi, inv_lo;
+    // constants of the tolerance arithmetic (FastArith, arith.cuh): (2/r, 2/rh),
+    // the halved kernel and gradient coefficients (C/2, G/2) of both scales, the
+    // viscosity's 0.01 h^2 and 2 h alpha c for h = r, (r + rh)/2, rh, and the wall
+    // weight's 0.02 c^2
+    float2 fTor, fC, fG;
+    float3 fEps, fKv;
+    float fKw;
 };
 
 // Division by a per-scene constant b (the smoothing lengths), correctly rounded:

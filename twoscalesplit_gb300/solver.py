@@ -158,6 +158,20 @@ class Solver:
     def set_launch(self, shape):
         self._check(self.lib.tss_solver_set_launch(self.h, ctypes.byref(_abi.TssLaunch.from_dict(shape))))
 
+    @property
+    def arith(self):
+        """The gathers' arithmetic: "exact" (the reference's bits, the default) or
+        "fast" (within the step's 1e-5 tolerance; tss_solver_set_arith)."""
+        m = ctypes.c_int(0)
+        self._check(self.lib.tss_solver_get_arith(self.h, ctypes.byref(m)))
+        return "fast" if m.value == _abi.TSS_ARITH_FAST else "exact"
+
+    def set_arith(self, mode):
+        if mode not in ("exact", "fast"):
+            raise ValueError("arith must be 'exact' or 'fast'")
+        self._check(self.lib.tss_solver_set_arith(
+            self.h, _abi.TSS_ARITH_FAST if mode == "fast" else _abi.TSS_ARITH_EXACT))
+
     def autotune(self, steps_per_trial=3):
         """Time every candidate launch shape on this handle's own steps and install
         the fastest per gather (tss_solver_autotune).  The trial steps advance the

@@ -29,7 +29,7 @@ def lib():
     return _abi.load_library()
 
 
-def _inputs(n, cells, seed):
+def _inputs(n, seed):
     rng = np.random.default_rng(seed)
     pos = rng.uniform(-0.05, 1.05, size=(n, 2)).astype(np.float32)  # includes clamped points
     ids = rng.permutation(3 * n)[:n].astype(np.int32)
@@ -61,13 +61,38 @@ def _run(lib, pos, ids, dims, noalloc):
 def test_noalloc_grid_build_matches_workspace_entry_point_on_consecutive_calls(lib):
     # two different problems back to back through the shared array
     for n, cells, seed in ((200_000, 700, 1), (37_013, 256, 2)):
-        pos, ids = _inputs(n, cells, seed)
+        pos, ids = _inputs(n, seed)
         ref_order, ref_off = _run(lib, pos, ids, (cells, cells), noalloc=False)
         got_order, got_off = _run(lib, pos, ids, (cells, cells), noalloc=True)
         # integer outputs: the tolerance is exact equality
         assert np.array_equal(got_off, ref_off)
         assert np.array_equal(got_order, ref_order)
         assert got_off[0] == 0 and got_off[-1] == n
+
+
+def test_noalloc_grid_build_empty_and_near_the_limit(lib):
+    # n = 0: every cell empty, the offsets all zero
+    order, off = _run(lib, np.zeros((0, 2), np.float32), np.zeros(0, np.int32), (64, 64), noalloc=True)
+    assert order.shape == (0,) and np.array_equal(off, np.zeros(64 * 64 + 1, np.int32))
+    # the largest problem of this grid whose workspace still fits the array, twice in a row
+    dims = (1400, 1400)
+    ws = ctypes.c_size_t(0)
+    lo, hi = 1, 8_000_000
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        assert lib.tss_grid_workspace_size(mid, dims[0], dims[1], ctypes.byref(ws)) == 0
+        if ws.value <= _abi.TSS_GRID_NOALLOC_MAX_BYTES:
+            lo = mid
+        else:
+            hi = mid - 1
+    n = lo
+    assert lib.tss_grid_workspace_size(n + 1, dims[0], dims[1], ctypes.byref(ws)) == 0
+    assert ws.value > _abi.TSS_GRID_NOALLOC_MAX_BYTES
+    pos, ids = _inputs(n, 5)
+    ref_order, ref_off = _run(lib, pos, ids, dims, noalloc=False)
+    for _ in range(2):
+        got_order, got_off = _run(lib, pos, ids, dims, noalloc=True)
+        assert np.array_equal(got_off, ref_off) and np.array_equal(got_order, ref_order)
 
 
 def test_noalloc_grid_build_refuses_sizes_beyond_its_array(lib):

@@ -81,7 +81,13 @@ __global__ void __launch_bounds__(kScanThreads) k_grid_scan(GridBufs g) {
         }
         unsigned sum = 0;
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) sum += v[k];
+        for (int k = 0; k < kScanItems; ++k) {
+            sum += v[k];
+            if (v[k] > static_cast<unsigned>(kBigCell)) {  // ordered by a block sort in the reorder
+                const int slot = atomicAdd(g.nbig, 1);
+                if (slot < g.big_cap) g.big[slot] = base + k;
+            }
+        }
         unsigned inc = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -147,6 +153,10 @@ __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __r
                                unsigned* err) {
     const int n = *n_ptr;
     const int total = *g.total;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the scan's list of big cells, for the reorder
+        *g.nbig_snap = *g.nbig;
+        *g.nbig = 0;  // empty for the next build's scan
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int c = g.key[i];
         if (c < 0) continue;  // dropped from the list
@@ -163,9 +173,132 @@ __global__ void k_grid_scatter(const int* __restrict__ n_ptr, const int32_t* __r
     }
 }
 
+namespace {
+
+// Gathers list entry src's state into sorted position dst.
+__device__ __forceinline__ void reorder_move(const ReorderArgs& a, int src, int dst, int id, unsigned* err) {
+    if (a.dst_pos) a.dst_pos[dst] = a.src_pos[src];
+    if (a.src_vel) a.dst_vel[dst] = a.src_vel[src];
+    if (a.src_st) {
+        uint8_t st = a.src_st[src];
+        a.dst_st[dst] = st;
+        if (a.h_state0 && (st & 1u) == 0u) *a.h_state0 = 1;
+    }
+    if (a.dst_id) a.dst_id[dst] = id;
+    if (a.src_dens) {
+        a.dst_dens[dst] = a.src_dens[src];
+        a.dst_pres[dst] = a.src_pres[src];
+    }
+    if (a.dst_order) a.dst_order[dst] = src;
+    if (a.dst_sc) a.dst_sc[dst] = a.page_scene[(id >> a.id_shift) >> a.page_shift];
+    if (a.slot_map) {
+        if (id >= 0 && id < a.slots) a.slot_map[id] = dst;
+        else atomicOr(err, kErrGridIndex);
+    }
+}
+
+// Sorts the ids of k entries (perm[0..k).y, non-negative) ascending with the whole
+// block (kReorderThreads threads): least-significant-digit radix sort, 8-bit
+// digits, as many passes as the largest id needs, between buffers x and y (k ints
+// each, global memory).  Each pass is a block histogram, its exclusive scan, and a
+// stable scatter of the entries in tiles of kReorderThreads, taken in order: an
+// entry's place is its digit's running base + the same-digit entries of earlier
+// warps in the tile + its rank among its warp's same-digit lanes.  Returns the
+// buffer holding the sorted ids.  Every thread of the block must call it.
+__device__ const int* block_sort_ids(const int2* __restrict__ perm, int k, int* x, int* y) {
+    constexpr int kWarps = kReorderThreads / 32;
+    __shared__ unsigned s_base[256];
+    __shared__ unsigned s_wcnt[kWarps][256];
+    __shared__ unsigned s_max[kWarps];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned mx = 0;
+    for (int i = t; i < k; i += kReorderThreads) {
+        const int id = perm[i].y;
+        x[i] = id;
+        mx = max(mx, static_cast<unsigned>(id));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_max[warp] = mx;
+    for (int w = 0; w < kWarps; ++w) s_wcnt[w][t] = 0u;
+    __syncthreads();
+    mx = 0;
+    for (int w = 0; w < kWarps; ++w) mx = max(mx, s_max[w]);
+    const int bits = 32 - __clz(static_cast<int>(mx | 1u));
+    const int passes = (bits + 7) / 8;
+    const unsigned lt = (1u << lane) - 1u;
+    int* in = x;
+    int* out = y;
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = 8 * pass;
+        s_base[t] = 0u;
+        __syncthreads();
+        for (int i = t; i < k; i += kReorderThreads) atomicAdd(&s_base[(in[i] >> shift) & 255], 1u);
+        __syncthreads();
+        // exclusive scan of the 256 digit counts (one per thread)
+        const unsigned c = s_base[t];
+        unsigned inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) s_max[warp] = inc;
+        __syncthreads();
+        unsigned before = 0;
+        for (int w = 0; w < warp; ++w) before += s_max[w];
+        s_base[t] = before + inc - c;
+        __syncthreads();
+        for (int t0 = 0; t0 < k; t0 += kReorderThreads) {
+            const int i = t0 + t;
+            const bool valid = i < k;
+            const int v = valid ? in[i] : 0;
+            const unsigned dg = static_cast<unsigned>(v >> shift) & 255u;
+            // lanes past k take keys no digit has, so they group with nothing
+            const unsigned peers = __match_any_sync(0xffffffffu, valid ? dg : 256u + lane);
+            const unsigned r = __popc(peers & lt);
+            if (valid && r == 0) s_wcnt[warp][dg] = __popc(peers);
+            __syncthreads();
+            if (valid) {
+                unsigned dst = s_base[dg] + r;
+                for (int w = 0; w < warp; ++w) dst += s_wcnt[w][dg];
+                out[dst] = v;
+            }
+            __syncthreads();
+            unsigned sum = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                sum += s_wcnt[w][t];
+                s_wcnt[w][t] = 0u;
+            }
+            s_base[t] += sum;
+            __syncthreads();
+        }
+        int* tmp = in;
+        in = out;
+        out = tmp;
+    }
+    return in;
+}
+
+// the number of entries of sorted[0..k) below id
+__device__ __forceinline__ int lower_rank(const int* __restrict__ sorted, int k, int id) {
+    int lo = 0, hi = k;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sorted[mid] < id) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+}  // namespace
+
 // The sorted entries are [0, total); the list count *n_ptr becomes total (only
-// block 0 writes it, and nothing in this kernel reads it).
-__global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, unsigned* err) {
+// block 0 writes it, and nothing in this kernel reads it).  Entries of cells with
+// at most kBigCell entries are placed by counting the smaller ids of their cell;
+// the bigger cells (listed by the scan) are placed whole by one block each.
+__global__ void __launch_bounds__(kReorderThreads) k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a,
+                                                                  unsigned* err) {
     const int n = *g.total;
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_ptr = n;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -185,40 +318,50 @@ __global__ void k_grid_reorder(int* n_ptr, int cap, GridBufs g, ReorderArgs a, u
             atomicOr(err, kErrGridIndex);
             continue;
         }
+        if (e - s > kBigCell) continue;  // placed below, with its cell
         int r = 0;
         for (int j = s; j < e; ++j) r += g.perm[j].y < id;
-        const int dst = s + r;
-        a.dst_pos[dst] = a.src_pos[src];
-        if (a.src_vel) a.dst_vel[dst] = a.src_vel[src];
-        if (a.src_st) {
-            uint8_t st = a.src_st[src];
-            a.dst_st[dst] = st;
-            if (a.h_state0 && (st & 1u) == 0u) *a.h_state0 = 1;
+        reorder_move(a, src, s + r, id, err);
+    }
+    const int nb = min(*g.nbig_snap, g.big_cap);
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const int c = g.big[b];
+        if (c < 0 || c >= g.ncells) {
+            if (threadIdx.x == 0) atomicOr(err, kErrGridIndex);
+            continue;
         }
-        if (a.dst_id) a.dst_id[dst] = id;
-        if (a.src_dens) {
-            a.dst_dens[dst] = a.src_dens[src];
-            a.dst_pres[dst] = a.src_pres[src];
+        const int s = g.off[c], e = g.off[c + 1];
+        if (s < 0 || e > n || e - s <= kBigCell) {
+            if (threadIdx.x == 0) atomicOr(err, kErrGridIndex);
+            continue;
         }
-        if (a.dst_order) a.dst_order[dst] = src;
-        if (a.dst_sc) a.dst_sc[dst] = a.page_scene[(id >> a.id_shift) >> a.page_shift];
-        if (a.slot_map) {
-            if (id >= 0 && id < a.slots) a.slot_map[id] = dst;
-            else atomicOr(err, kErrGridIndex);
+        const int k = e - s;
+        const int* sorted = block_sort_ids(g.perm + s, k, g.rank + s, g.sortbuf + s);
+        __syncthreads();
+        for (int j = threadIdx.x; j < k; j += blockDim.x) {
+            const int2 pe = g.perm[s + j];
+            const int src = pe.x, id = pe.y;
+            if (src < 0 || src >= cap) {
+                atomicOr(err, kErrGridIndex);
+                continue;
+            }
+            reorder_move(a, src, s + lower_rank(sorted, k, id), id, err);
         }
+        __syncthreads();  // the buffers are reused by the block's next cell
     }
 }
 
-size_t grid_bufs_bytes(int cap, int ncells) {
+size_t grid_bufs_bytes(int cap, int ncells, bool own_off) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     int ntiles = (ncells + kScanTile - 1) / kScanTile;
     if (ntiles < 1) ntiles = 1;
-    return al(sizeof(unsigned) * (size_t)ncells) + al(sizeof(int) * ((size_t)ncells + 1)) +
-           al(sizeof(int) * (size_t)cap) * 2 + al(sizeof(int2) * (size_t)cap) + al(sizeof(unsigned) * (size_t)ntiles) +
-           256;
+    const size_t big_cap = static_cast<size_t>(cap) / (kBigCell + 1) + 1;
+    return al(sizeof(unsigned) * (size_t)ncells) + (own_off ? al(sizeof(int) * ((size_t)ncells + 1)) : 0) +
+           al(sizeof(int) * (size_t)cap) * 3 + al(sizeof(int2) * (size_t)cap) + al(sizeof(unsigned) * (size_t)ntiles) +
+           al(sizeof(int) * big_cap) + 256;
 }
 
-GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
+GridBufs grid_bufs_carve(void* base, int cap, int ncells, bool own_off) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     char* p = static_cast<char*>(base);
     GridBufs g;
@@ -227,18 +370,28 @@ GridBufs grid_bufs_carve(void* base, int cap, int ncells) {
     if (g.ntiles < 1) g.ntiles = 1;
     g.count = reinterpret_cast<unsigned*>(p);
     p += al(sizeof(unsigned) * (size_t)ncells);
-    g.off = reinterpret_cast<int*>(p);
-    p += al(sizeof(int) * ((size_t)ncells + 1));
+    g.off = nullptr;
+    if (own_off) {
+        g.off = reinterpret_cast<int*>(p);
+        p += al(sizeof(int) * ((size_t)ncells + 1));
+    }
     g.key = reinterpret_cast<int*>(p);
     p += al(sizeof(int) * (size_t)cap);
     g.rank = reinterpret_cast<int*>(p);
+    p += al(sizeof(int) * (size_t)cap);
+    g.sortbuf = reinterpret_cast<int*>(p);
     p += al(sizeof(int) * (size_t)cap);
     g.perm = reinterpret_cast<int2*>(p);
     p += al(sizeof(int2) * (size_t)cap);
     g.tile_sum = reinterpret_cast<unsigned*>(p);
     p += al(sizeof(unsigned) * (size_t)g.ntiles);
+    g.big_cap = cap / (kBigCell + 1) + 1;
+    g.big = reinterpret_cast<int*>(p);
+    p += al(sizeof(int) * static_cast<size_t>(g.big_cap));
     g.used = nullptr;
-    g.total = reinterpret_cast<int*>(p);
+    g.total = reinterpret_cast<int*>(p);  // the last 256 bytes: total, nbig, nbig_snap
+    g.nbig = g.total + 1;
+    g.nbig_snap = g.total + 2;
     return g;
 }
 
@@ -259,7 +412,7 @@ cudaError_t grid_sort_enqueue(const int32_t* id, int* n_ptr, int cap, GridBufs g
     k_grid_scan<<<sb, kScanThreads, 0, stream>>>(g);
     if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
     k_grid_scatter<<<pb, T, 0, stream>>>(n_ptr, id, g, err);
-    k_grid_reorder<<<pb, T, 0, stream>>>(n_ptr, cap, g, a, err);
+    k_grid_reorder<<<pb, kReorderThreads, 0, stream>>>(n_ptr, cap, g, a, err);
     return cudaGetLastError();
 }
 
@@ -270,6 +423,7 @@ cudaError_t grid_build_enqueue(const float2* pos, const int32_t* id, int* n_ptr,
     if ((e = cudaMemsetAsync(g.count, 0, sizeof(unsigned) * static_cast<size_t>(g.ncells), stream)) != cudaSuccess)
         return e;
     if ((e = cudaMemsetAsync(g.tile_sum, 0, sizeof(unsigned) * g.ntiles, stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(g.nbig, 0, sizeof(int), stream)) != cudaSuccess) return e;
     if ((e = grid_keys_enqueue(pos, n_ptr, cap, ox, oy, cell, dimx, dimy, g, stream)) != cudaSuccess) return e;
     return grid_sort_enqueue(id, n_ptr, cap, g, a, err, stream);
 }
@@ -282,11 +436,12 @@ __global__ void k_set_int(int* p, int v) { *p = v; }
 // C ABI: grid build on caller-owned device memory
 // ---------------------------------------------------------------------------
 namespace {
-// workspace layout: [n + error word (256 B)] [grid buffers] [scratch pos copy]
+// workspace layout: [n + error word (256 B)] [grid buffers without the offset
+// table, which is the caller's d_cell_off]
 size_t ws_bytes(int n, int dimx, int dimy) {
     size_t cells = static_cast<size_t>(dimx) * static_cast<size_t>(dimy);
     int cap = n > 0 ? n : 1;
-    return 256 + tss::grid_bufs_bytes(cap, static_cast<int>(cells)) + ((sizeof(float2) * (size_t)cap + 255) & ~size_t(255));
+    return 256 + tss::grid_bufs_bytes(cap, static_cast<int>(cells), false);
 }
 }  // namespace
 
@@ -310,14 +465,12 @@ extern "C" tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, in
     char* w = static_cast<char*>(d_workspace);
     int* n_dev = reinterpret_cast<int*>(w);
     unsigned* err = reinterpret_cast<unsigned*>(n_dev + 2);
-    tss::GridBufs g = tss::grid_bufs_carve(w + 256, cap, cells);
+    tss::GridBufs g = tss::grid_bufs_carve(w + 256, cap, cells, false);
     g.off = d_cell_off;  // write the offsets straight into the caller's table
-    float2* scratch = reinterpret_cast<float2*>(w + 256 + tss::grid_bufs_bytes(cap, cells));
     if (cudaMemsetAsync(w, 0, 256, st) != cudaSuccess) return TSS_CUDA_ERROR;
     tss::k_set_int<<<1, 1, 0, st>>>(n_dev, n);
-    tss::ReorderArgs a{};
+    tss::ReorderArgs a{};  // only the order is gathered
     a.src_pos = reinterpret_cast<const float2*>(d_pos);
-    a.dst_pos = scratch;
     a.dst_order = d_order;
     cudaError_t e = tss::grid_build_enqueue(reinterpret_cast<const float2*>(d_pos), d_id, n_dev, cap, origin_x, origin_y,
                                             cell_size, dimx, dimy, g, a, err, st);

@@ -17,9 +17,16 @@
 //                   next build; off[used] = total = the number of keyed entries
 //   k_grid_scatter  perm[off[key[i]] + rank[i]] = (i, id[i]); entries whose key is
 //                   negative (removed since their key pass) are dropped
-//   k_grid_reorder  each sorted slot counts the smaller ids of its cell to find its
-//                   final place and gathers the particle's state there (SoA reorder);
-//                   the list count becomes the sorted count
+//   k_grid_reorder  each sorted slot finds its final place in its cell, ascending
+//                   id, and gathers the particle's state there (SoA reorder); the
+//                   list count becomes the sorted count.  In a cell of at most
+//                   kBigCell entries the slot counts the smaller ids of its cell
+//                   (k compares, the grids' cells hold a few particles); a larger
+//                   cell -- particles clamped into a border cell, a collapsing flow,
+//                   a caller's clustered points -- is taken whole by one block,
+//                   which sorts its ids (LSD radix sort, 8-bit digits, O(k) per
+//                   pass) and places each entry by a binary search, so no cell
+//                   costs more than O(k log k)
 #pragma once
 #include "tss_device.cuh"
 
@@ -32,6 +39,10 @@ namespace tss {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
+// Cells with more entries than this are ordered by a block-wide sort of their ids
+// in the reorder (see above); at most total / (kBigCell + 1) cells can be that big.
+constexpr int kBigCell = 32;
+constexpr int kReorderThreads = 256;
 
 struct GridBufs {
     int ncells;             // C
@@ -45,6 +56,11 @@ struct GridBufs {
     const int* used;        // device int: cells [0, used) can hold entries (null: all C); the
                             // scan covers only those, so its cost follows the cells in use
     int* total;             // device int: entries sorted by the last build
+    int* big;               // [big_cap] cells with more than kBigCell entries (the scan appends)
+    int big_cap;            // cap / (kBigCell + 1) + 1
+    int* nbig;              // device int: cells appended by the scan (the scatter resets it)
+    int* nbig_snap;         // device int: ... as the scatter found it, for the reorder
+    int* sortbuf;           // [cap] ids of the big cells while they are sorted (with rank)
 };
 
 // What the reorder moves: list-order arrays (src) into sorted-order arrays (dst).
@@ -107,8 +123,10 @@ __device__ __forceinline__ void grid_key(unsigned* __restrict__ count, int* __re
     if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&tile_sum[t], static_cast<unsigned>(__popc(peers)));
 }
 
-size_t grid_bufs_bytes(int cap, int ncells);
-GridBufs grid_bufs_carve(void* base, int cap, int ncells);
+// Device bytes of a grid's buffers for `cap` entries and `ncells` cells; own_off =
+// false leaves out the offset table (the caller then sets g.off to its own).
+size_t grid_bufs_bytes(int cap, int ncells, bool own_off = true);
+GridBufs grid_bufs_carve(void* base, int cap, int ncells, bool own_off = true);
 
 int particle_blocks(int cap, int threads);
 int sm_count();

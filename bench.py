@@ -3,27 +3,38 @@
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A "step" is one WCSPHSolver::AdvanceTS-equivalent step of the whole scene (grids,
-relaxation, densities, forces, splits, integration).  W warm-up steps run first,
-then the gathers' launch-shape autotuner (its trial steps are warm-up too; the
-shape changes no result); the scene is then reset to its initial state and
-exactly K steps (default 500, the 1M dam break's step count) are timed, each
-bracketed by CUDA events on the launching stream with L2 flushed (a 512 MiB write)
-between steps.  value = sum over the timed steps of the particles processed
-(n_low + n_high at each step) / device time.  e2e repeats the timed run through
-the C ABI with host buffers: the initial state is uploaded from pinned memory and
-every step's particle positions are read back to pinned memory (an overlapped
-read-back per step, double-buffered: staged on the device, then copied to host
-memory while the next step runs).
+relaxation, densities, forces, splits, integration).  The default workload,
+dam_break_1m_developed, is the 1M dam break (707 x 1414 low-res particles, region
+of interest [0.4,0.9]x[0,0.5], high-res pool 4M) from a developed state: the
+library runs it from the initial lattice until its high-res list holds 1M
+particles (~32,000 steps, untimed; make_workload), so that the timed steps carry
+both scales at scale -- ~1M low-res and ~1M high-res particles, the front still
+splitting.  --scene dam_break_1m times the initial lattice instead.
+
+W warm-up steps run first, then the gathers' launch-shape autotuner (its trial
+steps are warm-up too; the shape changes no result); the scene is then reset to
+its start state and exactly K steps (default 500, the 1M dam break's step count)
+are timed, each bracketed by CUDA events on the launching stream with L2 flushed (a
+512 MiB write) between steps.  value = sum over the timed steps of the particles
+processed (n_low + n_high at each step) / device time, in the exact arithmetic
+(the reference's bits).  The same K steps are then timed in the tolerance
+arithmetic (TSS_ARITH_FAST) and reported under "fast_arith".  e2e repeats each
+timed run through the C ABI with host buffers: the start state is uploaded from
+pinned memory and every step's particle positions are read back to pinned memory
+(an overlapped read-back per step, double-buffered: staged on the device, then
+copied to host memory while the next step runs).
 
 With N > 1 (torchrun) every rank runs an independent replica of the scene
 (replicas only: one scene does not shard); value sums the ranks' particle-steps
 over the slowest rank's time.
 
 --impl reference times the CPU restatement of the reference step (the oracle,
-FP32, OpenMP over all host threads) on the same scene; the reference itself is
-CUDA code with an OpenGL front end and has no CPU implementation of its own.  Its
-line also carries "rebuilt_cuda": the reference's own kernels rebuilt for sm_103a
-and run on the same scene by a headless restatement of AdvanceTS.
+FP32, OpenMP over all host threads) from the same start state; the reference
+itself is CUDA code with an OpenGL front end and has no CPU implementation of its
+own.  Its line also carries "rebuilt_cuda": the reference's own kernels rebuilt
+for sm_103a and run from the same start state by a headless restatement of
+AdvanceTS.  The developed start state is made on the GPU by this library in both
+arms (untimed setup).
 """
 import argparse
 import json
@@ -179,14 +190,91 @@ def _dist():
     return world, rank, local
 
 
-def cpu_baseline(scene_name, seed, budget_s, threads=None):
-    """The oracle (FP32, the reference's arithmetic) timed on the host cores."""
+# ---------------------------------------------------------------------------
+# plain workloads: a scene and the state its timed steps start from
+# ---------------------------------------------------------------------------
+# name -> (scene generator, high-res particles the start state must hold)
+DEVELOPED = {"dam_break_1m_developed": ("dam_break_1m", 1_000_000)}
+DEVELOP_CHUNK = 1000
+DEVELOP_MAX_STEPS = 80_000
+
+
+def make_workload(name, seed, cache=None):
+    """The scene of a plain workload and, for a developed one, the state its timed
+    steps start from: the scene run from its initial state by this library (exact
+    arithmetic, the tether guard on) until its high-res list holds the target count,
+    checked every DEVELOP_CHUNK steps.  The 1M dam break's block fills [0,0.4]x
+    [0,0.8] and its region of interest is [0.4,0.9]x[0,0.5], so from the initial
+    lattice nothing splits for thousands of steps; after ~32,000 steps (0.23 s of
+    flow at dt = 7.07e-6) the front has carried 250,000 parents through the region
+    and the pool holds 1M children.  Returns (scene, start) with start None for
+    the initial state.  `cache`: an .npz file the start state is read from when it
+    exists and written to otherwise (so that a profiler run can skip the
+    development)."""
+    from twoscalesplit_gb300 import _abi, scenes
+    if name not in DEVELOPED:
+        return scenes.make_scene(name, seed=seed), None
+    from twoscalesplit_gb300.solver import Solver
+    base, target = DEVELOPED[name]
+    sc = scenes.make_scene(base, seed=seed)
+    sc.config.flags |= _abi.TSS_FLAG_TETHER_GUARD
+    sc.name = name
+    keys = ("id", "pos", "vel", "state", "dens", "pres")
+    if cache and os.path.exists(cache):
+        z = np.load(cache)
+        start = {"low": {k: z["low_" + k] for k in keys}, "high": {k: z["high_" + k] for k in keys},
+                 "fresh": z["fresh"], "develop_steps": int(z["develop_steps"]), "develop_s": 0.0}
+        return sc, start
+    sol = Solver.from_scene(sc)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < DEVELOP_MAX_STEPS:
+        sol.step(DEVELOP_CHUNK)
+        steps += DEVELOP_CHUNK
+        if sol.counts()["n_high"] >= target:
+            break
+    sol.sync()  # raises on a device error
+    c = sol.counts()
+    if c["n_high"] < target:
+        raise RuntimeError(f"{name}: {c['n_high']} high-res particles after {steps} steps")
+    start = {"low": sol.download(0), "high": sol.download(1), "fresh": sol.get_fresh(), "develop_steps": steps,
+             "develop_s": time.perf_counter() - t0}
+    sol.close()
+    if cache:
+        np.savez(cache, fresh=start["fresh"], develop_steps=steps,
+                 **{f"{s}_{k}": start[s][k] for s in ("low", "high") for k in keys})
+    return sc, start
+
+
+def load_start(obj, sc, start):
+    """Put a solver or oracle in the workload's start state."""
+    from twoscalesplit_gb300.solver import Solver
+    if start is None:
+        low = {"id": np.arange(sc.n_low, dtype=np.int32), "pos": sc.low_pos, "vel": sc.low_vel,
+               "state": np.zeros(sc.n_low, np.uint8)}
+        high = {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32),
+                "vel": np.zeros((0, 2), np.float32), "state": np.zeros(0, np.uint8)}
+        fresh = np.zeros(0, np.int32)
+    else:
+        low, high, fresh = start["low"], start["high"], start["fresh"]
+    if isinstance(obj, Solver):
+        obj.upload(0, low)
+        obj.upload(1, high)
+        obj.set_fresh(fresh)
+    else:
+        for s, d in ((0, low), (1, high)):
+            obj.set_scale(s, d["id"], d["pos"], d["vel"], d["state"], d.get("dens"), d.get("pres"))
+        obj.set_fresh(fresh)
+
+
+def cpu_baseline(sc, start, budget_s, threads=None):
+    """The oracle (FP32, the reference's arithmetic) timed on the host cores, from
+    the workload's start state."""
     import oracle as O
-    from twoscalesplit_gb300 import scenes
     if threads:
         O.set_threads(threads)
-    sc = scenes.make_scene(scene_name, seed=seed)
     orc = O.Oracle(sc, 32)
+    load_start(orc, sc, start)
     done, parts, t0 = 0, 0, time.perf_counter()
     while True:
         n = orc.get(0, "id").shape[0] + orc.get(1, "id").shape[0]
@@ -196,9 +284,20 @@ def cpu_baseline(scene_name, seed, budget_s, threads=None):
         if time.perf_counter() - t0 >= budget_s or done >= sc.steps:
             break
     dt = time.perf_counter() - t0
+    where = "the initial state" if start is None else f"the developed state ({start['develop_steps']} steps)"
     return {"value": parts / dt, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-            "sample": f"{scene_name}: first {done} steps from the initial state ({parts} particle-steps, "
-                      f"{dt:.1f} s), FP32 CPU restatement of the reference step, OpenMP"}
+            "sample": f"{sc.name}: {done} steps from {where} ({parts} particle-steps, {dt:.1f} s), FP32 CPU "
+                      f"restatement of the reference step, OpenMP"}
+
+
+def survey_step_bytes(n_low, n_high, c_low, c_high, splits):
+    """Algorithmic bytes of one step in the radix-sort model of the hot-path survey:
+    per scale N (120 + 16 k) + 8 C with k = ceil(ceil(log2 C) / 8) digit passes,
+    plus 72 per split (the config-1 figure of 0.87 GB/step assumes a full 4M pool)."""
+    def k(c):
+        return math.ceil(math.ceil(math.log2(max(c, 2))) / 8)
+    return (n_low * (120 + 16 * k(c_low)) + 8 * c_low + n_high * (120 + 16 * k(c_high)) + 8 * c_high
+            + 72 * splits)
 
 
 def tuned_shape(sol, kind, n_low, args):
@@ -217,18 +316,32 @@ def compact_shape(shape):
             for g, v in shape.items()}
 
 
+def workload_config(sc, start, args):
+    """The config keys both arms report for a plain workload."""
+    cfg = sc.config
+    c = {"workload": sc.name, "n_low": sc.n_low, "cap_high": sc.cap_high, "dt": cfg.dt,
+         "relax_iters": cfg.relax_iters, "q1_compat": bool(cfg.flags & 1),
+         "tether_guard": bool(cfg.flags & 4), "seed": 0,
+         "start": "initial lattice" if start is None else
+                  f"developed: {start['develop_steps']} steps of the library from the initial lattice"}
+    if start is not None:
+        c["n_high_start"] = int(start["high"]["id"].shape[0])
+    return c
+
+
 def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
         return
     budget = float(os.environ.get("TSS_REF_BUDGET_S", "150"))
     import oracle as O
-    from twoscalesplit_gb300 import scenes
-    sc = scenes.make_scene(args.scene, seed=0)
+    sc, start = make_workload(args.scene, 0, args.start_cache)
     orc = O.Oracle(sc, 32)
+    load_start(orc, sc, start)
     for _ in range(min(args.warmup, 1)):
         orc.step()
     orc = O.Oracle(sc, 32)
+    load_start(orc, sc, start)
     t0 = time.perf_counter()
     parts = 0
     steps = 0
@@ -240,31 +353,44 @@ def run_reference(args):
             break
     dt = time.perf_counter() - t0
     v = parts / dt
+    where = "the initial state" if start is None else \
+        f"the developed state (made on the GPU by this library, untimed: {start['develop_steps']} steps)"
+    conf = workload_config(sc, start, args)
+    conf.update({"l2": "n/a (CPU)", "launch": "n/a (CPU)", "autotune_steps": 0, "parallelism": "replicas1",
+                 "arith": "exact (FP32, the reference's arithmetic)"})
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.scene, "n_low": sc.n_low, "cap_high": sc.cap_high, "l2": "n/a (CPU)"},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": conf,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-                             "sample": f"{args.scene}: first {steps} of the {args.steps} requested steps from the "
-                                       f"initial state, bounded to {budget:.0f} s"},
+                             "sample": f"{sc.name}: first {steps} of the {args.steps} requested steps from {where}, "
+                                       f"bounded to {budget:.0f} s"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    line["rebuilt_cuda"] = rebuilt_reference_gpu(sc, args)
+    line["rebuilt_cuda"] = rebuilt_reference_gpu(sc, start, args)
     print(json.dumps(line), flush=True)
 
 
-def rebuilt_reference_gpu(sc, args, budget_s=30.0):
+def rebuilt_reference_gpu(sc, start, args, budget_s=30.0):
     """The reference's own CUDA kernels rebuilt for sm_103a (oracle RefGPU: its
     kernel source as a cubin, driven by a headless restatement of AdvanceTS) timed
-    on this GPU on the same scene, or why not.  Each reference step ends in its
-    three synchronous count read-backs, so the wall clock per step is its step
+    on this GPU from the same start state, or why not.  Each reference step ends in
+    its three synchronous count read-backs, so the wall clock per step is its step
     time; the run is bounded to `budget_s`."""
     try:
         import oracle as O
         if not O.refgpu_available():
             return {"unavailable": "the reference's kernels for sm_103a are not built here (no cubin or no driver)"}
-        ref = O.RefGPU(sc)
+
+        def fresh_ref():
+            r = O.RefGPU(sc)
+            if start is not None:
+                r.set_state(start["low"], start["high"])
+            return r
+
+        ref = fresh_ref()
         ref.step(max(args.warmup, 1))
-        ref = O.RefGPU(sc)  # timed from the initial state, like the other arms
+        del ref
+        ref = fresh_ref()  # timed from the start state, like the other arms
+        c0 = ref.counts()
         parts, steps = 0, 0
         t0 = time.perf_counter()
         while steps < args.steps:
@@ -277,15 +403,125 @@ def rebuilt_reference_gpu(sc, args, budget_s=30.0):
         dt = time.perf_counter() - t0
         c = ref.counts()
         return {"value": parts / dt, "unit": UNIT, "ms_per_step": 1e3 * dt / steps, "steps": steps,
-                "n_high_end": c["n_high"],
+                "n_high_start": c0["n_high"], "n_high_end": c["n_high"],
                 "build": "TwoScale2D/WCSPHSolver.cu kernels (lines 14-2283) for sm_103a, nvcc -O3 with the "
                          "reference's defaults (contraction on); texture fetches as bounded loads",
                 "split_region": "x > 0.5, hard-coded in the reference's kernels (WCSPHSolver.cu:1835), not the "
                                 "scene's region of interest",
-                "timing": "wall clock per step from the initial state, including the reference's three "
+                "timing": "wall clock per step from the workload's start state, including the reference's three "
                           "synchronous count read-backs and its thrust sorts (no rendering)"}
     except Exception as e:  # the arm's CPU line stands without it
         return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def timed_steps(sol, K, reset, flush, stream, sh, world):
+    """K steps, each between CUDA events on the launching stream, L2 flushed before
+    each; returns (device ms, wall s, clocks sampled meanwhile)."""
+    import torch
+    reset()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    _, _, local = _dist()
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+    clocks = ClockSampler(vis[local].strip() if local < len(vis) and vis[local].strip()
+                          else (str(local) if world > 1 else None))
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for k in range(K):
+        flush.zero_()
+        evs[k][0].record(stream)
+        sol.step(1, stream=sh)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    sol.sync()  # raises on a device error (capacity, NaN, grid index)
+    return sum(a.elapsed_time(b) for a, b in evs), wall, clk
+
+
+def stage_average(sol, reset, flush, sh, n):
+    """Stage times of the profiling graph averaged over the first n steps from the
+    start state (L2 flushed before each)."""
+    from twoscalesplit_gb300 import _abi
+    sol.profile(True)
+    reset()
+    acc = {k: 0.0 for k in _abi.STAGE_NAMES}
+    for _ in range(n):
+        flush.zero_()
+        sol.step(1, stream=sh)
+        for name, v in sol.stage_times().items():
+            acc[name] += v
+    sol.profile(False)
+    return {k: v / n for k, v in acc.items()}
+
+
+def e2e_run(sol, sc, start, K, sh, world):
+    """The timed steps end to end through the C ABI with host buffers: the start
+    state (both lists) is uploaded from page-locked memory, and every step's
+    positions (both lists) are read back into page-locked memory by
+    tss_solver_read_positions_async (staged on the device on the step's stream,
+    then copied to host memory on the solver's own stream while the next step
+    runs), double-buffered: the host waits for step k's read-back (its ticket)
+    before it reuses that buffer at step k + 2, and counts the bytes it received.
+    Returns (seconds, h2d bytes, d2h bytes)."""
+    import ctypes
+
+    import torch
+    from twoscalesplit_gb300 import _abi
+    from twoscalesplit_gb300._abi import TssScaleState, fptr
+    load_start(sol, sc, start)
+    cap_h = max(sc.cap_high, 1)
+    outs = [(torch.empty((sc.n_low, 2), dtype=torch.float32).pin_memory(),
+             torch.empty((cap_h, 2), dtype=torch.float32).pin_memory(),
+             torch.zeros(2, dtype=torch.int32).pin_memory()) for _ in range(2)]
+    sol.step(1, stream=sh)  # keep the graph captured and the staging buffers allocated outside the timed region
+    sol.read_wait(sol.read_positions_async(outs[0][0], outs[0][1], outs[0][2], stream=sh))
+    torch.cuda.synchronize()
+    if start is None:
+        lists = [{"id": np.arange(sc.n_low, dtype=np.int32), "pos": sc.low_pos, "vel": sc.low_vel,
+                  "state": np.zeros(sc.n_low, np.uint8)},
+                 {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32),
+                  "vel": np.zeros((0, 2), np.float32), "state": np.zeros(0, np.uint8)}]
+        fresh = np.zeros(0, np.int32)
+    else:
+        lists = [start["low"], start["high"]]
+        fresh = start["fresh"]
+    pinned = [{k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in d.items()
+               if k in ("id", "pos", "vel", "state")} for d in lists]
+    states = [TssScaleState(int(d["id"].shape[0]), _abi.iptr(d["id"].numpy()), fptr(d["pos"].numpy()),
+                            fptr(d["vel"].numpy()), _abi.u8ptr(d["state"].numpy()), None, None) for d in pinned]
+    lib = sol.lib
+    h2d = sum(int(d["id"].shape[0]) * (4 + 8 + 8 + 1) for d in lists) + 4 * fresh.shape[0]
+    d2h = 0
+    tickets = [None, None]
+
+    def received(b):
+        sol.read_wait(tickets[b])
+        c = outs[b][2].tolist()
+        tickets[b] = None
+        return 8 * (min(c[0], sc.n_low) + min(c[1], cap_h)) + 8
+
+    if world > 1:
+        torch.distributed.barrier()
+    e0 = time.perf_counter()
+    for s in (0, 1):
+        _abi.check(lib.tss_solver_upload(sol.h, s, ctypes.byref(states[s])))
+    sol.set_fresh(fresh)
+    for k in range(K):
+        b = k % 2
+        if tickets[b] is not None:
+            d2h += received(b)
+        sol.step(1, stream=sh)
+        tickets[b] = sol.read_positions_async(outs[b][0], outs[b][1], outs[b][2], stream=sh)
+    for b in (K % 2, (K + 1) % 2):  # the older read-back first
+        if tickets[b] is not None:
+            d2h += received(b)
+    return time.perf_counter() - e0, h2d, d2h
 
 
 def run_ours(args):
@@ -297,169 +533,131 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
-    from twoscalesplit_gb300 import _abi, build, scenes
-    from twoscalesplit_gb300._abi import TssScaleState, fptr
+    from twoscalesplit_gb300 import _abi, build
     from twoscalesplit_gb300.solver import Solver
     build.build()
-    sc = scenes.make_scene(args.scene, seed=rank)
+    sc, start = make_workload(args.scene, rank, args.start_cache if rank == 0 else None)
     sol = Solver.from_scene(sc)
     # a dedicated stream: the graph replays, the L2 flush and the timing events all
     # go to it, so the events bracket exactly the step
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
-    init_low = sol.download(0)
-    empty = {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32), "vel": np.zeros((0, 2), np.float32),
-             "state": np.zeros(0, np.uint8)}
 
     def reset():
-        sol.upload(0, init_low)
-        sol.upload(1, empty)
-        sol.set_fresh(np.zeros(0, np.int32))
+        load_start(sol, sc, start)
 
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
-    # warm-up (graph capture happens here), then the launch-shape autotuner on the
-    # same state (its trial steps are warm-up too: the state is reset after them)
-    sol.step(max(args.warmup, 1), stream=sh)
-    torch.cuda.synchronize(dev)
-    shape, tune_steps = tuned_shape(sol, "single", sc.n_low, args)
-    reset()
+    kind = "single" if start is None else "single_developed"
     K = args.steps
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
-    clocks = ClockSampler(vis[local].strip() if local < len(vis) and vis[local].strip() else (str(local) if world > 1 else None))
-    clocks.start()
-    time.sleep(0.3)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize(dev)
-    w0 = time.perf_counter()
-    for k in range(K):
-        flush.zero_()
-        evs[k][0].record(stream)
-        sol.step(1, stream=sh)
-        evs[k][1].record(stream)
-    torch.cuda.synchronize(dev)
-    wall = time.perf_counter() - w0
-    if world > 1:
-        torch.distributed.barrier()
-    clk = clocks.stop()
-    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
-    sol.sync()  # raises on a device error (capacity, NaN, timeout)
-    # particles processed per step (deterministic replay, untimed)
+    legs = {}
+    for mode in ("exact", "fast"):
+        sol.set_arith(mode)
+        # warm-up (graph capture happens here), then the launch-shape autotuner on the
+        # same state (its trial steps are warm-up too: the state is reset after them)
+        reset()
+        sol.step(max(args.warmup, 1), stream=sh)
+        torch.cuda.synchronize(dev)
+        reset()
+        shape, tune_steps = tuned_shape(sol, kind if mode == "exact" else kind + "_fast", sc.n_low, args)
+        dev_ms, wall, clk = timed_steps(sol, K, reset, flush, stream, sh, world)
+        st_avg = stage_average(sol, reset, flush, sh, min(K, 50))
+        e2e_s, h2d, d2h = e2e_run(sol, sc, start, K, sh, world)
+        legs[mode] = {"dev_ms": dev_ms, "wall": wall, "clk": clk, "stage": st_avg, "e2e_s": e2e_s, "h2d": h2d,
+                      "d2h": d2h, "shape": shape, "tune_steps": tune_steps}
+        if args.exact_only:
+            break
+    sol.set_arith("exact")
+    # particles processed per step (deterministic replay of the exact steps, untimed)
     reset()
     counts = []
+    c0 = sol.counts()
     for k in range(K):
         c = sol.counts()
         counts.append(c["n_low"] + c["n_high"])
         sol.step(1, stream=sh)
     c_end = sol.counts()
     parts = float(sum(counts))
-    # stage times (profiling graph), averaged over a replay of the same steps
-    sol.profile(True)
-    reset()
-    st_sum = {k: 0.0 for k in _abi.STAGE_NAMES}
-    n_prof = min(K, 50)
-    for k in range(n_prof):
-        flush.zero_()
-        sol.step(1, stream=sh)
-        for name, v in sol.stage_times().items():
-            st_sum[name] += v
-    sol.profile(False)
-    st_avg = {k: v / n_prof for k, v in st_sum.items()}
-    # e2e through the C ABI with pinned host buffers: the initial state is uploaded
-    # from page-locked memory, and every step's positions (both lists) are read back
-    # into page-locked memory by tss_solver_read_positions_async (staged on the
-    # device on the step's stream, then copied to host memory on the solver's own
-    # stream while the next step runs), double-buffered: the host waits for step
-    # k's read-back (its ticket) before it reuses that buffer at step k + 2, and
-    # counts the bytes it received
-    reset()
-    cap_h = max(sc.cap_high, 1)
-    outs = [(torch.empty((sc.n_low, 2), dtype=torch.float32).pin_memory(),
-             torch.empty((cap_h, 2), dtype=torch.float32).pin_memory(),
-             torch.zeros(2, dtype=torch.int32).pin_memory()) for _ in range(2)]
-    sol.step(1, stream=sh)  # keep the graph captured and the staging buffers allocated outside the timed region
-    sol.read_wait(sol.read_positions_async(outs[0][0], outs[0][1], outs[0][2], stream=sh))
-    torch.cuda.synchronize(dev)
-    pin_low = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in init_low.items()}
-    tickets = [None, None]
-    lib = sol.lib
-    st_low = TssScaleState(sc.n_low, _abi.iptr(pin_low["id"].numpy()), fptr(pin_low["pos"].numpy()),
-                           fptr(pin_low["vel"].numpy()), _abi.u8ptr(pin_low["state"].numpy()), None, None)
-    import ctypes
-    d2h = 0
-    h2d = sc.n_low * (4 + 8 + 8 + 1)
-
-    def received(b):
-        sol.read_wait(tickets[b])
-        c = outs[b][2].tolist()
-        tickets[b] = None
-        return 8 * (min(c[0], sc.n_low) + min(c[1], cap_h)) + 8
-
-    if world > 1:
-        torch.distributed.barrier()
-    e0 = time.perf_counter()
-    _abi.check(lib.tss_solver_upload(sol.h, 0, ctypes.byref(st_low)))
-    sol.upload(1, empty)
-    sol.set_fresh(np.zeros(0, np.int32))
-    for k in range(K):
-        b = k % 2
-        if tickets[b] is not None:
-            d2h += received(b)
-        sol.step(1, stream=sh)
-        tickets[b] = sol.read_positions_async(outs[b][0], outs[b][1], outs[b][2], stream=sh)
-    for b in (K % 2, (K + 1) % 2):  # the older read-back first
-        if tickets[b] is not None:
-            d2h += received(b)
-    e2e_s = time.perf_counter() - e0
-    times = torch.tensor([dev_ms, e2e_s, parts], dtype=torch.float64, device=dev)
+    splits_per_step = (c_end["total_split"] - c0["total_split"]) / K
+    times = torch.tensor([legs["exact"]["dev_ms"], legs["exact"]["e2e_s"], parts], dtype=torch.float64, device=dev)
     if world > 1:
         t_max = times.clone()
         torch.distributed.all_reduce(t_max[:2], op=torch.distributed.ReduceOp.MAX)
         tot = times.clone()
         torch.distributed.all_reduce(tot[2:], op=torch.distributed.ReduceOp.SUM)
-        dev_ms, e2e_s, parts_all = float(t_max[0]), float(t_max[1]), float(tot[2])
+        parts_all = float(tot[2])
+        for leg in legs.values():  # the slowest rank's times (replicas of the same work)
+            tl = torch.tensor([leg["dev_ms"], leg["e2e_s"]], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(tl, op=torch.distributed.ReduceOp.MAX)
+            leg["dev_ms"], leg["e2e_s"] = float(tl[0]), float(tl[1])
     else:
         parts_all = parts
     if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
         return
-    value = parts_all / (dev_ms / 1e3)
     peak, peak_kind = hbm_peak()
     cfg = sc.config
     c_low, c_high = cfg.dims_low[0] * cfg.dims_low[1], cfg.dims_high[0] * cfg.dims_high[1]
     n_high_avg = float(np.mean(counts)) - sc.n_low
     carry = cfg.relax_iters > 0
-    top = max(st_avg, key=st_avg.get)
-    top_bytes = stage_bytes(top, sc.n_low, n_high_avg, c_low, c_high, carry, 0)
-    top_gbs = top_bytes / (st_avg[top] * 1e-3) / 1e9 if st_avg[top] > 0 else 0.0
-    step_bytes = sum(stage_bytes(s, sc.n_low, n_high_avg, c_low, c_high, carry, 0) for s in _abi.STAGE_NAMES)
-    step_ms = dev_ms / K
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
-        "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": args.scene, "n_low": sc.n_low, "n_high_end": c_end["n_high"],
-                   "cap_high": sc.cap_high, "dt": cfg.dt, "relax_iters": cfg.relax_iters,
-                   "q1_compat": bool(cfg.flags & 1), "l2": "flushed between timed steps (512 MiB write)",
-                   "parallelism": f"replicas{world}", "seed": 0, "launch": compact_shape(shape),
-                   "autotune_steps": tune_steps},
-        "roofline": {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
+
+    def roofline(leg):
+        st_avg = leg["stage"]
+        top = max(st_avg, key=st_avg.get)
+        top_bytes = stage_bytes(top, sc.n_low, n_high_avg, c_low, c_high, carry, 0)
+        top_gbs = top_bytes / (st_avg[top] * 1e-3) / 1e9 if st_avg[top] > 0 else 0.0
+        step_ms = leg["dev_ms"] / K
+        step_bytes = sum(stage_bytes(s, sc.n_low, n_high_avg, c_low, c_high, carry, 0) for s in _abi.STAGE_NAMES)
+        sv = survey_step_bytes(sc.n_low, n_high_avg, c_low, c_high, splits_per_step)
+        return top, {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
                      "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": measured_traffic(top),
                      "traffic_source": "profiles/dram_traffic.txt (ncu, one launch)",
                      "algorithmic_bytes_per_launch": top_bytes, "launch_ms": st_avg[top],
-                     "step": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (step_ms * 1e-3) / 1e9,
-                              "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak}},
-        "issue_roofline": issue_roofline(top, st_avg[top], (clk or {}).get("sm_mhz")),
-        "stage_ms": {k: round(v, 5) for k, v in st_avg.items()},
-        "e2e": {"value": parts_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / K,
-                "d2h_bytes_per_step": d2h / K},
-        "gpu_launches": K * (14 + 3 * cfg.relax_iters),  # kernels per step: 2 grids x 4, 5 gathers, finish
-        "clocks": clk,
-        "wall_s_timed": wall,
+                     "step": {"algorithmic_bytes": step_bytes,
+                              "achieved_gbs": step_bytes / (step_ms * 1e-3) / 1e9,
+                              "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak,
+                              "survey_model_bytes": sv,
+                              "survey_model_frac": sv / (step_ms * 1e-3) / 1e9 / peak}}
+
+    ex = legs["exact"]
+    top, roof = roofline(ex)
+    conf = workload_config(sc, start, args)
+    conf.update({"n_high_end": c_end["n_high"], "splits_per_step": splits_per_step,
+                 "l2": "flushed between timed steps (512 MiB write)", "parallelism": f"replicas{world}",
+                 "launch": compact_shape(ex["shape"]), "autotune_steps": ex["tune_steps"],
+                 "arith": "exact (FP32, the reference's arithmetic; bit-identical to it)"})
+    if start is not None:
+        conf["develop_s"] = round(start["develop_s"], 2)
+    line = {
+        "metric": METRIC, "value": parts_all / (ex["dev_ms"] / 1e3), "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ex["dev_ms"] / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": conf,
+        "roofline": roof,
+        "issue_roofline": issue_roofline(top, ex["stage"][top], (ex["clk"] or {}).get("sm_mhz")),
+        "stage_ms": {k: round(v, 5) for k, v in ex["stage"].items()},
+        "e2e": {"value": parts_all / ex["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": ex["h2d"] / K,
+                "d2h_bytes_per_step": ex["d2h"] / K},
+        # kernels per step: 2 grid sorts x 3 (scan, scatter, reorder), 4 gathers, split
+        # compaction, finish (+ 3 per relaxation sub-step); the 3 memset nodes are not counted
+        "gpu_launches": K * (12 + 3 * cfg.relax_iters),
+        "clocks": ex["clk"],
+        "wall_s_timed": ex["wall"],
     }
+    if "fast" in legs:
+        fa = legs["fast"]
+        ftop, froof = roofline(fa)
+        line["fast_arith"] = {
+            "what": "TSS_ARITH_FAST: per pair an approximate rsqrt and reciprocal and FMAs; densities, forces and "
+                    "positions within 1e-5 of the FP32 oracle per step (tests/test_gpu_fast_arith.py)",
+            "value": parts_all / (fa["dev_ms"] / 1e3), "unit": UNIT, "ms_per_step": fa["dev_ms"] / K,
+            "speedup_vs_exact": ex["dev_ms"] / fa["dev_ms"],
+            "e2e": {"value": parts_all / fa["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": fa["h2d"] / K,
+                    "d2h_bytes_per_step": fa["d2h"] / K},
+            "roofline": froof, "stage_ms": {k: round(v, 5) for k, v in fa["stage"].items()},
+            "launch": compact_shape(fa["shape"]), "clocks": fa["clk"]}
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.scene, 0, args.cpu_budget_s)
+        line["cpu_baseline"] = cpu_baseline(sc, start, args.cpu_budget_s)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -878,7 +1076,11 @@ def main():
                     help="timed steps (default: 500 plain, 1000 batch, 2000 adaptive -- the configs' step counts)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--scene", default="dam_break_1m")
+    ap.add_argument("--scene", default="dam_break_1m_developed",
+                    help="plain workload: dam_break_1m_developed (default), dam_break_1m or dam_break_5k")
+    ap.add_argument("--exact-only", action="store_true", help="plain workload: skip the fast-arithmetic leg")
+    ap.add_argument("--start-cache", default=None,
+                    help="plain workload: .npz of the developed start state (read if present, else written)")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "adaptive"])

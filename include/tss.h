@@ -49,6 +49,16 @@ typedef enum tss_status {
  * parent (dist == 0) gets 0/0 = NaN there.  With the flag such a child keeps its
  * position (the formula's limit: for dist below the tether radius it leaves the
  * child where it is).  Off by default: the reference's arithmetic. */
+#define TSS_FLAG_OLDER_PLACEMENT 0x8u
+/* TSS_FLAG_OLDER_PLACEMENT: place a split parent's four children as the reference's
+ * older snapshot does (TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:840-850): at the
+ * predicted position +-DIR_LEN * r on both diagonals, DIR_LEN = 0.35355339 (so each
+ * child sits r/2 from its parent), instead of the current tree's
+ * +-0.5*sqrt(m/(2 rho pi)) (WCSPHSolver.cu:956-1005).  The older snapshot relaxes
+ * the children so placed before they couple (relax_iters = 4); the current tree's
+ * placement puts them so close to their parent that the relaxation's first
+ * sub-step finds them at 2-3 rest densities.  The tether, the parent's place in the
+ * low-res list and the coupling stay the current tree's. */
 #define TSS_FLAG_MERGE 0x2u
 /* TSS_FLAG_MERGE: a split parent (low-res state 1) whose predicted position is
  * outside the region of interest returns to state 0, and its four children are
@@ -470,8 +480,11 @@ const char* tss_status_string(tss_status st);
  *   d_cell_off[C+1]  : dense offsets: particles of cell c are order[off[c]..off[c+1])
  *                      (the reference's cellStart/cellEnd, with empty cells as
  *                      empty ranges instead of -1)
- * d_id holds distinct ids (any non-negative int32); d_workspace is scratch of
- * tss_grid_workspace_size bytes.  Enqueued on `stream`; nothing is synchronised. */
+ * d_id holds distinct ids (any non-negative int32); with repeated ids d_order is
+ * undefined (entries are skipped or written twice; nothing outside the buffers is
+ * touched).  d_workspace is scratch of tss_grid_workspace_size bytes.  Enqueued on
+ * `stream`; nothing is synchronised.  Cells of any fullness cost O(k log k): cells
+ * of more than 32 entries are sorted by id in one block each. */
 tss_status tss_grid_workspace_size(int n, int dimx, int dimy, size_t* bytes);
 tss_status tss_grid_build(const float* d_pos, const int32_t* d_id, int n,
                           float origin_x, float origin_y, float cell_size,
@@ -516,12 +529,16 @@ tss_status tss_solver_render(tss_solver* s, const tss_view* view, const float* p
  * owned by its host's memory manager).  The caller still passes d_pos, d_id,
  * d_order and d_cell_off as for tss_grid_build.
  *   - Limit: tss_grid_workspace_size(n, dimx, dimy) must not exceed
- *     TSS_GRID_NOALLOC_MAX_BYTES (32 MiB, e.g. 500,000 particles on a 1400x1400
- *     grid); larger problems get TSS_CAPACITY and should use tss_grid_build.
+ *     TSS_GRID_NOALLOC_MAX_BYTES (32 MiB: up to 1,277,759 particles on a
+ *     1400x1400 grid); larger problems get TSS_CAPACITY and should use
+ *     tss_grid_build.
  *   - The array occupies TSS_GRID_NOALLOC_MAX_BYTES on every GPU that loads the
  *     library, until the process exits.
  *   - The first call on a device looks up the array's device address on that
- *     device; make that first call before any stream capture.
+ *     device; make that first call before any stream capture.  The address is
+ *     kept for the life of the process: after cudaDeviceReset the library's
+ *     module is loaded again and the kept address is stale, so do not call this
+ *     entry point after resetting a device.
  *   - All calls share the array: calls whose work overlaps on the GPU (other
  *     streams, other host threads) race and give undefined results.  Each call
  *     clears the parts that must start at zero. */

@@ -35,6 +35,7 @@ def _orc_lib():
         lib.orc_set_scale.argtypes = [vp, i, i, vp, vp, vp, vp, vp, vp]
         lib.orc_set_fresh.argtypes = [vp, i, vp]
         lib.orc_set_steps.argtypes = [vp, ctypes.c_longlong]
+        lib.orc_set_want_scale.argtypes = [vp, i]
         lib.orc_splat.argtypes = [vp, i, i, i, vp, vp, i, f, vp, f, vp]
         lib.orc_step.argtypes = [vp]
         lib.orc_get.argtypes = [vp, i, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
@@ -63,8 +64,21 @@ def _ref_lib():
         lib.ref_step.argtypes = [vp]
         lib.ref_get.argtypes = [vp, i, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         lib.ref_grid.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
+        lib.ref_older_children.argtypes = [f, i, f, f, f, f, vp, vp]
         _REF = lib
     return _REF
+
+
+def ref_older_children(r, pid, pos, vel):
+    """The older snapshot's own child placement (initSubParticlesAndAddToList,
+    TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:813-867) compiled for the CPU: the
+    four children's positions and velocities (4 x 2 float32 each)."""
+    lib = _ref_lib()
+    p8 = np.zeros(8, np.float32)
+    v8 = np.zeros(8, np.float32)
+    lib.ref_older_children(float(r), int(pid), float(pos[0]), float(pos[1]), float(vel[0]), float(vel[1]),
+                           _p(p8), _p(v8))
+    return p8.reshape(4, 2), v8.reshape(4, 2)
 
 
 def refcpu_available():
@@ -159,6 +173,11 @@ class Oracle:
     def set_steps(self, steps):
         """Steps taken so far (the moving region of interest's step index)."""
         self.lib.orc_set_steps(self.h, int(steps))
+
+    def set_want_scale(self, on=True):
+        """Compute each acceleration's error scale in the next steps: the sum of the
+        magnitudes of its summands (get(scale, "acc_scale"))."""
+        self.lib.orc_set_want_scale(self.h, 1 if on else 0)
 
     def step(self):
         return self.lib.orc_step(self.h)
@@ -278,6 +297,8 @@ def _refgpu_lib():
         lib.refgpu_counts.argtypes = [vp, vp]
         lib.refgpu_state.restype = i
         lib.refgpu_state.argtypes = [vp, i, vp, vp, vp, i]
+        lib.refgpu_set_state.restype = i
+        lib.refgpu_set_state.argtypes = [vp, vp, vp, vp, i, vp, vp, vp, vp, ctypes.c_char_p, i]
         _REFGPU = (lib, cubin)
     return _REFGPU
 
@@ -316,6 +337,27 @@ class RefGPU:
         err = ctypes.create_string_buffer(512)
         if self.lib.refgpu_step(self.h, int(n), err, 512) != 0:
             raise RuntimeError("refgpu_step: " + err.value.decode(errors="replace"))
+
+    def set_state(self, low, high):
+        """Replace the state with another solver's (list-order dicts of id, pos, vel,
+        state per scale, as Solver.download returns them): every low-res slot must be
+        present; split parents (state 1) form the transient list."""
+        n = self.scene.n_low
+        lid = np.asarray(low["id"], np.int64)
+        if lid.shape[0] != n or not np.array_equal(np.sort(lid), np.arange(n)):
+            raise ValueError("set_state needs every low-res slot")
+        lp = np.zeros((n, 2), np.float32)
+        lv = np.zeros((n, 2), np.float32)
+        ls = np.zeros(n, np.uint8)
+        lp[lid], lv[lid], ls[lid] = low["pos"], low["vel"], low["state"]
+        hid = np.ascontiguousarray(high["id"], np.int32)
+        hp = np.ascontiguousarray(high["pos"], np.float32)
+        hv = np.ascontiguousarray(high["vel"], np.float32)
+        hs = np.ascontiguousarray(high["state"], np.uint8)
+        err = ctypes.create_string_buffer(512)
+        if self.lib.refgpu_set_state(self.h, _p(lp), _p(lv), _p(ls), hid.shape[0], _p(hid), _p(hp), _p(hv), _p(hs),
+                                     err, 512) != 0:
+            raise RuntimeError("refgpu_set_state: " + err.value.decode(errors="replace"))
 
     def counts(self):
         c = np.zeros(3, np.int32)

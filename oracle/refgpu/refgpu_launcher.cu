@@ -254,6 +254,51 @@ struct RefGpu {
         return true;
     }
 
+    // Replaces the particle state with a state taken elsewhere (a developed scene),
+    // kept as the reference keeps it: slot-indexed arrays, the active low id list
+    // holding every low-res slot (split parents stay in it), the active high id
+    // list the given high-res slots, and the active transient list every split
+    // parent (each step re-appends them, WCSPHSolver.cu:1135-1140).  low_* have
+    // L.max entries by slot; high_* are in list order.
+    bool set_state(const float* low_pos, const float* low_vel, const unsigned char* low_st, int n_high,
+                   const int* high_ids, const float* high_pos, const float* high_vel, const unsigned char* high_st) {
+        if (n_high < 0 || n_high > H.max) return fail("set_state: high-res count out of range");
+        const size_t nl = static_cast<size_t>(L.max), nh = static_cast<size_t>(H.max);
+        std::vector<float> hp(2 * nh, 0.0f), hv(2 * nh, 0.0f);
+        std::vector<unsigned char> hs(nh, 0);
+        std::vector<int> tr;
+        for (int k = 0; k < n_high; ++k) {
+            const int id = high_ids[k];
+            if (id < 0 || id >= H.max) return fail("set_state: high-res id out of range");
+            hp[2 * id] = high_pos[2 * k];
+            hp[2 * id + 1] = high_pos[2 * k + 1];
+            hv[2 * id] = high_vel[2 * k];
+            hv[2 * id + 1] = high_vel[2 * k + 1];
+            hs[id] = high_st[k];
+        }
+        for (int i = 0; i < L.max; ++i)
+            if (low_st[i] == 1) tr.push_back(i);
+        std::vector<int> lid(nl);
+        for (int i = 0; i < L.max; ++i) lid[i] = i;
+        const int a = active;
+        bool ok = rt(cudaMemcpy(L.pos, low_pos, sizeof(float) * 2 * nl, cudaMemcpyHostToDevice), "set_state") &&
+                  rt(cudaMemcpy(L.vel, low_vel, sizeof(float) * 2 * nl, cudaMemcpyHostToDevice), "set_state") &&
+                  rt(cudaMemcpy(stL, low_st, nl, cudaMemcpyHostToDevice), "set_state") &&
+                  rt(cudaMemcpy(gL.ids[a], lid.data(), sizeof(int) * nl, cudaMemcpyHostToDevice), "set_state") &&
+                  rt(cudaMemcpy(H.pos, hp.data(), sizeof(float) * 2 * nh, cudaMemcpyHostToDevice), "set_state") &&
+                  rt(cudaMemcpy(H.vel, hv.data(), sizeof(float) * 2 * nh, cudaMemcpyHostToDevice), "set_state") &&
+                  rt(cudaMemcpy(stH, hs.data(), nh, cudaMemcpyHostToDevice), "set_state");
+        if (ok && n_high > 0)
+            ok = rt(cudaMemcpy(gH.ids[a], high_ids, sizeof(int) * n_high, cudaMemcpyHostToDevice), "set_state");
+        if (ok && !tr.empty())
+            ok = rt(cudaMemcpy(trL[a], tr.data(), sizeof(int) * tr.size(), cudaMemcpyHostToDevice), "set_state");
+        if (!ok) return false;
+        L.num = L.max;
+        H.num = n_high;
+        nTrL = static_cast<int>(tr.size());
+        return rt(cudaDeviceSynchronize(), "set_state");
+    }
+
     bool create(const char* cubin, const tss_config* c, int n_low, const float* low_pos, const float* low_vel,
                 float mass_low, int cap_high, float mass_high, int n_wall, const float* wall_pos, float mass_wall) {
         cfg = *c;
@@ -347,6 +392,18 @@ int refgpu_step(void* h, int n, char* err, int err_len) {
             if (err && err_len > 0) std::snprintf(err, static_cast<size_t>(err_len), "%s", r->err.c_str());
             return 1;
         }
+    return 0;
+}
+
+// Replaces the state (RefGpu::set_state).  0 on success, else 1 with the reason in err.
+int refgpu_set_state(void* h, const float* low_pos, const float* low_vel, const unsigned char* low_state,
+                     int n_high, const int* high_ids, const float* high_pos, const float* high_vel,
+                     const unsigned char* high_state, char* err, int err_len) {
+    RefGpu* r = static_cast<RefGpu*>(h);
+    if (!r->set_state(low_pos, low_vel, low_state, n_high, high_ids, high_pos, high_vel, high_state)) {
+        if (err && err_len > 0) std::snprintf(err, static_cast<size_t>(err_len), "%s", r->err.c_str());
+        return 1;
+    }
     return 0;
 }
 

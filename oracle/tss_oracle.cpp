@@ -77,6 +77,7 @@ struct Consts {
     bool q1;
     bool merge;    // TSS_FLAG_MERGE: split parents outside the ROI merge back
     bool tether_guard;  // TSS_FLAG_TETHER_GUARD: no 0/0 when a child sits on its parent
+    bool older_place;   // TSS_FLAG_OLDER_PLACEMENT: children at +-DIR_LEN*r (older snapshot 840-850)
 };
 
 // computeGridCoordinate(pos, offset), WCSPHSolver.cu:265-289.
@@ -164,6 +165,7 @@ struct Scale {
     std::vector<V2<T>> s_pos, s_vel, s_acc;
     std::vector<uint8_t> s_st;
     std::vector<T> s_dens, s_pres, s_q;  // q = p / rho^2
+    std::vector<T> s_scale;              // |summands| of each acceleration (want_scale only)
     std::vector<int32_t> map;            // slot id -> sorted index, -1 if absent
     int n() const { return (int)id.size(); }
 };
@@ -247,6 +249,7 @@ public:
         k.q1 = (c.flags & TSS_FLAG_Q1_COMPAT) != 0;
         k.merge = (c.flags & TSS_FLAG_MERGE) != 0;
         k.tether_guard = (c.flags & TSS_FLAG_TETHER_GUARD) != 0;
+        k.older_place = (c.flags & TSS_FLAG_OLDER_PLACEMENT) != 0;
         slotsL = nL_slots;
         slotsH = 4 * nL_slots;
         capH = cap_high;
@@ -535,6 +538,36 @@ public:
         accT.y += lw * pij.y * (w + w2) / T(2);
     }
 
+    // The error scale of an acceleration, against which a per-step tolerance on it
+    // is stated: the sum of the magnitudes of its summands (m |pressure/viscosity
+    // term| over both scales' pairs, sigma |tension term|, |wall term|, g), where a
+    // pressure term's magnitude also counts how far it moves when the two densities
+    // move by their own relative amount (kappa = |d(p/rho^2)/d rho| rho, from the
+    // Tait equation).  Each summand carries its own rounding, and near rest density
+    // the Tait equation turns a density's last-place rounding into a large relative
+    // change of its pressure, so an FP32 evaluation is only accurate to a few units
+    // of this scale however small the acceleration: a result within tol * scale is
+    // the exact sum for densities and summands each within tol relative.  Computed
+    // only when want_scale is set (a separate pass; the step's results do not
+    // depend on it).
+    bool want_scale = false;
+    inline T eos_kappa(T q, T dens) const {
+        const T a = dens / k.rho0;
+        const T a3 = a * a * a;
+        return std::fabs(T(7) * k.B * a3 * a3 / (k.rho0 * dens) - T(2) * q / dens);
+    }
+    inline void pair_mag(V2<T> pij, T dist, V2<T> vij, T qi, T qj, T densi, T densj, T h, T lw, T& ma,
+                         T& mt) const {
+        T visc = T(0);
+        T dvp = vij.x * pij.x + vij.y * pij.y;
+        if (dvp < T(0)) visc = dvp / (dist * dist + T(0.01f) * h * h) * T(2) * h * k.alpha * k.cs / (densi + densj);
+        const T cmag = std::fabs(qi) + std::fabs(qj) + std::fabs(visc) + eos_kappa(qi, densi) + eos_kappa(qj, densj);
+        V2<T> gI = dW(pij, dist, k.r, k.GL);
+        V2<T> gJ = dW(pij, dist, k.rh, k.GH);
+        ma += std::fabs(lw) * cmag * std::hypot(gI.x + gJ.x, gI.y + gJ.y) / T(2);
+        mt += std::fabs(lw) * std::hypot(pij.x, pij.y) * std::fabs(W(dist, k.r, k.CL) + W(dist, k.rh, k.CH)) / T(2);
+    }
+
     // ---- low-res force, predicted advance, split (1648-1865, 1604-1646, 956-1005) ----
     std::vector<uint8_t> nxt_stL;
     std::vector<V2<T>> nxt_posL, nxt_velL;
@@ -544,6 +577,7 @@ public:
         nxt_posL.resize(n);
         nxt_velL.resize(n);
         std::vector<uint8_t> flag(n, 0);
+        if (want_scale) L.s_scale.assign(n, T(0));
         const T hx = (k.r + k.rh) / T(2);
         // the region of interest of this step (a rectangle moving by roi_vdt per step)
         const T kf = T(steps_done);
@@ -555,6 +589,7 @@ public:
             uint8_t s = L.s_st[i];
             T dens = L.s_dens[i], qi = L.s_q[i];
             V2<T> acc{0, 0}, accH{0, 0}, accT{0, 0}, accB{0, 0};
+            T sa = 0, sah = 0, stn = 0, sb = 0;  // error scale (want_scale)
             int csx, csy, cex, cey;
             coord<T>(p.x, p.y, -k.r, k.ox, k.oy, k.r, k.dimL, csx, csy);
             coord<T>(p.x, p.y, k.r, k.ox, k.oy, k.r, k.dimL, cex, cey);
@@ -568,6 +603,8 @@ public:
                             float lw = del_w(L.s_st[j]);
                             V2<T> vij{v.x - L.s_vel[j].x, v.y - L.s_vel[j].y};
                             pair_force(pij, dist, vij, qi, L.s_q[j], dens, L.s_dens[j], k.r, T(lw), acc, accT);
+                            if (want_scale)
+                                pair_mag(pij, dist, vij, qi, L.s_q[j], dens, L.s_dens[j], k.r, T(lw), sa, stn);
                         }
                     }
                     for (int b = wall_off[h]; b < wall_off[h + 1]; ++b) {
@@ -576,6 +613,7 @@ public:
                         T gm = gamma_wall(dist, k.r, k.cs);
                         accB.x += k.cBL * gm * pik.x;
                         accB.y += k.cBL * gm * pik.y;
+                        if (want_scale) sb += std::fabs(k.cBL * gm) * std::hypot(pik.x, pik.y);
                     }
                 }
             coord<T>(p.x, p.y, -k.r, k.ox, k.oy, k.rh, k.dimH, csx, csy);
@@ -591,6 +629,8 @@ public:
                         if (dist != T(0) && dist < k.r) {
                             V2<T> vij{v.x - H.s_vel[j].x, v.y - H.s_vel[j].y};
                             pair_force(pij, dist, vij, qi, H.s_q[j], dens, H.s_dens[j], hx, T(lw), accH, accT);
+                            if (want_scale)
+                                pair_mag(pij, dist, vij, qi, H.s_q[j], dens, H.s_dens[j], hx, T(lw), sah, stn);
                         }
                     }
                 }
@@ -606,6 +646,7 @@ public:
             acc.y += accB.y;
             acc.y -= k.g;
             L.s_acc[i] = acc;
+            if (want_scale) L.s_scale[i] = k.mL * sa + k.mH * sah + k.sigma * stn + sb + std::fabs(k.g);
             v.x += k.dt * acc.x;
             v.y += k.dt * acc.y;
             p.x += k.dt * v.x;
@@ -631,6 +672,7 @@ public:
         const int n = H.n();
         nxt_posH.resize(n);
         nxt_velH.resize(n);
+        if (want_scale) H.s_scale.assign(n, T(0));
         const T hx = (k.r + k.rh) / T(2);
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; ++i) {
@@ -638,6 +680,7 @@ public:
             uint8_t s = H.s_st[i];
             T dens = H.s_dens[i], qi = H.s_q[i];
             V2<T> acc{0, 0}, accL{0, 0}, accT{0, 0}, accB{0, 0};
+            T sa = 0, sal = 0, stn = 0, sb = 0;  // error scale (want_scale)
             int csx, csy, cex, cey;
             coord<T>(p.x, p.y, -k.rh, k.ox, k.oy, k.rh, k.dimH, csx, csy);
             coord<T>(p.x, p.y, k.rh, k.ox, k.oy, k.rh, k.dimH, cex, cey);
@@ -652,6 +695,8 @@ public:
                         if (dist != T(0) && dist < k.rh) {
                             V2<T> vij{v.x - H.s_vel[j].x, v.y - H.s_vel[j].y};
                             pair_force(pij, dist, vij, qi, H.s_q[j], dens, H.s_dens[j], k.rh, T(lw), acc, accT);
+                            if (want_scale)
+                                pair_mag(pij, dist, vij, qi, H.s_q[j], dens, H.s_dens[j], k.rh, T(lw), sa, stn);
                         }
                     }
                 }
@@ -669,6 +714,8 @@ public:
                         if (dist != T(0) && dist < k.r) {
                             V2<T> vij{v.x - L.s_vel[j].x, v.y - L.s_vel[j].y};
                             pair_force(pij, dist, vij, qi, L.s_q[j], dens, L.s_dens[j], hx, T(lw), accL, accT);
+                            if (want_scale)
+                                pair_mag(pij, dist, vij, qi, L.s_q[j], dens, L.s_dens[j], hx, T(lw), sal, stn);
                         }
                     }
                     for (int b = wall_off[h]; b < wall_off[h + 1]; ++b) {
@@ -677,6 +724,7 @@ public:
                         T gm = gamma_wall(dist, k.rh, k.cs);
                         accB.x += k.cBH * gm * pik.x;
                         accB.y += k.cBH * gm * pik.y;
+                        if (want_scale) sb += std::fabs(k.cBH * gm) * std::hypot(pik.x, pik.y);
                     }
                 }
             acc.x *= -k.mH;
@@ -691,6 +739,7 @@ public:
             acc.y += accB.y;
             acc.y -= k.g;
             H.s_acc[i] = acc;
+            if (want_scale) H.s_scale[i] = k.mH * sa + k.mL * sal + k.sigma * stn + sb + std::fabs(k.g);
             v.x += k.dt * acc.x;
             v.y += k.dt * acc.y;
             p.x += k.dt * v.x;
@@ -765,7 +814,10 @@ public:
             int id = L.s_id[i];
             V2<T> p = nxt_posL[i], v = nxt_velL[i];
             T rho = L.s_dens[i];
-            T rad = T(0.5 * std::sqrt(double(k.mL) / (double(T(2) * rho) * kPi)));
+            // the older snapshot's placement: pos +- DIR_LEN*h with h = r, in float
+            // (TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:840-850)
+            T rad = k.older_place ? T(0.35355339f * float(k.r))
+                                  : T(0.5 * std::sqrt(double(k.mL) / (double(T(2) * rho) * kPi)));
             const V2<T> cp[4] = {{p.x + rad, p.y + rad}, {p.x - rad, p.y + rad},
                                  {p.x + rad, p.y - rad}, {p.x - rad, p.y - rad}};
             for (int c = 0; c < 4; ++c) {
@@ -867,6 +919,7 @@ int get_buf(Oracle<T>& o, int scale, const char* name, void* dst, size_t cap, si
     if (nm == "dens") return put_s(S.s_dens);
     if (nm == "pres") return put_s(S.s_pres);
     if (nm == "acc") return put_v(S.s_acc);
+    if (nm == "acc_scale") return put_s(S.s_scale);
     if (nm == "split") return put_i(o.split);
     if (nm == "fresh") return put_i(o.fresh);
     if (nm == "wall_cell_off") return put_i(o.wall_off);
@@ -959,6 +1012,13 @@ int orc_splat(const float* view, int W, int H, int n, const float* pos, const fl
 int orc_set_steps(void* p, long long steps) {
     Handle* h = (Handle*)p;
     if (h->f) h->f->steps_done = steps; else h->d->steps_done = steps;
+    return TSS_OK;
+}
+
+// Whether the next steps also compute each acceleration's error scale ("acc_scale").
+int orc_set_want_scale(void* p, int on) {
+    Handle* h = (Handle*)p;
+    if (h->f) h->f->want_scale = on != 0; else h->d->want_scale = on != 0;
     return TSS_OK;
 }
 

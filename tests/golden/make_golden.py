@@ -12,6 +12,14 @@ from the reference checkout by oracle/refcpu/build_ref.sh) and run headless:
                       dam-break state with high-res particles and transient parents
   step_q1_relax.npz   the same with the relaxation of the previous step's children
                       (TwoScale2D-master/TwoScale2D/WCSPHSolver.cu:2380-2446)
+  step_developed_51k.npz
+                      one AdvanceTS of the reference's kernels from a developed
+                      51,200-particle dam break (160 x 320 lattice, region x > 0.5,
+                      mass calibrated to rest density): 7,000 steps of flow, 5,644
+                      split parents and 22,576 children, Q1 on.  The state is
+                      developed by the oracle (bit-identical to the reference's
+                      kernels on this schedule, tests/test_oracle_cpu.py) and the
+                      recorded step is the reference's own
 
 Run from the repository root on a machine with the reference checkout:
     python tests/golden/make_golden.py
@@ -67,14 +75,30 @@ def _ref_state(ref, scale):
                 pres=ref.get(scale, "pres")[ids])
 
 
-def step_case(fname, relax_iters, warm_steps):
-    sc = scenes.dam_break_small(20, 40, seed=7, relax_iters=relax_iters, calibrate_mass=False)
+def step_case(fname, relax_iters, warm_steps, nx=20, ny=40, calibrate_mass=False, seed=7, develop_oracle=False):
+    sc = scenes.dam_break_small(nx, ny, seed=seed, relax_iters=relax_iters, calibrate_mass=calibrate_mass)
     sc.config.roi[:] = REF_ROI
     ref = O.RefCPU(sc)
-    for _ in range(warm_steps):
-        ref.step()
-    fresh = ref.get(0, "split")
-    inp = {s: _ref_state(ref, s) for s in (0, 1)}
+    if develop_oracle:  # the oracle develops the state, the reference's kernels take the recorded step
+        orc = O.Oracle(sc, 32)
+        for _ in range(warm_steps):
+            orc.step()
+        for s in (0, 1):
+            st = orc.state(s)
+            dens, pres = (st["dens_state"], st["pres_state"]) if relax_iters > 0 else (None, None)
+            ref.set_scale(s, st["id"], st["pos"].astype(np.float32), st["vel"].astype(np.float32), st["state"],
+                          dens, pres)
+        ref.set_fresh(orc.get(0, "fresh"))
+        fresh = orc.get(0, "fresh")
+        inp = {s: {"id": orc.state(s)["id"], "pos": orc.state(s)["pos"].astype(np.float32),
+                   "vel": orc.state(s)["vel"].astype(np.float32), "state": orc.state(s)["state"],
+                   "dens": orc.state(s)["dens_state"].astype(np.float32),
+                   "pres": orc.state(s)["pres_state"].astype(np.float32)} for s in (0, 1)}
+    else:
+        for _ in range(warm_steps):
+            ref.step()
+        fresh = ref.get(0, "split")
+        inp = {s: _ref_state(ref, s) for s in (0, 1)}
     ref.step()
     out = {}
     c = sc.config
@@ -110,3 +134,4 @@ if __name__ == "__main__":
     grid_cases()
     step_case("step_q1.npz", 0, 120)
     step_case("step_q1_relax.npz", 4, 120)
+    step_case("step_developed_51k.npz", 0, 7000, nx=160, ny=320, calibrate_mass=True, seed=11, develop_oracle=True)

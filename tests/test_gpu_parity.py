@@ -39,7 +39,7 @@ def _torch():
 
 
 # --------------------------------------------------------------------------- grid
-def _grid_gpu(pos, ids, origin, cell, dims):
+def _grid_gpu(pos, ids, origin, cell, dims, timing=None):
     torch = _torch()
     lib = _abi.load_library()
     n = ids.shape[0]
@@ -50,13 +50,19 @@ def _grid_gpu(pos, ids, origin, cell, dims):
     ws = ctypes.c_size_t(0)
     assert lib.tss_grid_workspace_size(n, int(dims[0]), int(dims[1]), ctypes.byref(ws)) == 0
     work = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    ev[0].record()
     st = lib.tss_grid_build(ctypes.c_void_p(dpos.data_ptr()), ctypes.c_void_p(did.data_ptr()), n,
                             float(origin[0]), float(origin[1]), float(cell), int(dims[0]), int(dims[1]),
                             ctypes.c_void_p(order.data_ptr()), ctypes.c_void_p(off.data_ptr()),
                             ctypes.c_void_p(work.data_ptr()), ws.value,
                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    ev[1].record()
     assert st == 0
     torch.cuda.synchronize()
+    if timing is not None:
+        timing.append(ev[0].elapsed_time(ev[1]))
     return order.cpu().numpy()[:n], off.cpu().numpy()
 
 
@@ -83,6 +89,34 @@ def test_grid_build_matches_oracle_adversarial(n, cells, spread):
     o_order, o_off = O.grid(pos, ids, (0.0, 0.0), 1.0 / cells, dims)
     assert np.array_equal(off, o_off)
     assert np.array_equal(order, o_order)
+
+
+@pytest.mark.parametrize("case", ["border_clamped", "one_cluster", "around_threshold"])
+def test_grid_build_crowded_cells_bounded(case):
+    """Cells far fuller than a grid's few particles per cell -- points outside the
+    domain clamped into its border cells (computeGridCoordinate,
+    WCSPHSolver.cu:247-248), a collapsed cluster, cells straddling the size where the
+    in-cell ordering switches from counting to a block sort -- give exactly the
+    stable (cell, id) order of the oracle, and the build stays fast (its time is
+    printed; an ordering quadratic in the cell size would take minutes here)."""
+    rng = np.random.default_rng({"border_clamped": 11, "one_cluster": 12, "around_threshold": 13}[case])
+    if case == "border_clamped":  # 1.2M points, ~300k in each corner cell of a 64x64 grid on [0,1]^2
+        n, dims, lo, hi = 1_200_000, (64, 64), -100.0, 101.0
+    elif case == "one_cluster":  # 400k points in ~650 cells of a 512x512 grid: ~600 per cell
+        n, dims, lo, hi = 400_000, (512, 512), 0.0, 0.05
+    else:  # ~38 per cell on average: cells both below and above the switch
+        n, dims, lo, hi = 100_000, (512, 512), 0.0, 0.1
+    pos = rng.uniform(lo, hi, size=(n, 2)).astype(np.float32)
+    ids = rng.permutation(2 * n)[:n].astype(np.int32)
+    ms = []
+    order, off = _grid_gpu(pos, ids, (0.0, 0.0), 1.0 / dims[0], dims, timing=ms)
+    o_order, o_off = O.grid(pos, ids, (0.0, 0.0), 1.0 / dims[0], dims)
+    assert np.array_equal(off, o_off)
+    assert np.array_equal(order, o_order)
+    counts = np.diff(off)
+    print(f"{case}: n={n}, largest cell {counts.max()}, build {ms[0]:.3f} ms")
+    assert counts.max() > 32
+    assert ms[0] < 1000.0
 
 
 # --------------------------------------------------------------------------- helpers
@@ -119,7 +153,7 @@ def _compare_step_buffers(gpu, orc, where):
 
 
 # --------------------------------------------------------------------------- step vs reference
-@pytest.mark.parametrize("fname", ["step_q1.npz", "step_q1_relax.npz"])
+@pytest.mark.parametrize("fname", ["step_q1.npz", "step_q1_relax.npz", "step_developed_51k.npz"])
 def test_step_matches_reference_fixture(fname):
     g = np.load(os.path.join(GOLDEN, fname))
     sc = scene_from_fixture(g)
@@ -152,7 +186,7 @@ def test_step_matches_reference_fixture(fname):
 
 
 # --------------------------------------------------------------------------- multi-step vs oracle
-@pytest.mark.parametrize("relax,flags,roi", [(4, 1, None), (0, 1, "ref"), (4, 0, None)])
+@pytest.mark.parametrize("relax,flags,roi", [(4, 1, None), (0, 1, "ref"), (4, 0, None), (4, 1 | 8, None)])
 def test_multistep_matches_oracle(relax, flags, roi):
     sc = scenes.dam_break_small(16, 32, seed=21, relax_iters=relax, flags=flags, calibrate_mass=(roi != "ref"))
     if roi == "ref":
@@ -186,6 +220,23 @@ def test_dam_break_5k_tracks_oracle_300_steps():
     _compare_step_buffers(sol, orc, 299)
     _assert_state_equal(sol, orc, TSS_SCALE_LOW, 299)
     _assert_state_equal(sol, orc, TSS_SCALE_HIGH, 299)
+    assert sol.counts()["n_high"] > 0
+
+
+def test_relaxed_cfg0_tracks_oracle():
+    """dam_break_5k with the older snapshot's child placement and relaxation: the GPU
+    equals the FP32 oracle bit for bit through splits and relaxation sub-steps."""
+    sc = scenes.dam_break_5k_relaxed(seed=3)
+    sol = Solver.from_scene(sc)
+    orc = O.Oracle(sc, 32)
+    for k in range(400):
+        orc.step()
+    sol.step(400)
+    sol.sync()
+    _compare_step_buffers(sol, orc, 399)
+    _assert_state_equal(sol, orc, TSS_SCALE_LOW, 399)
+    _assert_state_equal(sol, orc, TSS_SCALE_HIGH, 399)
+    assert np.array_equal(sol.get_fresh(), orc.get(0, "fresh"))
     assert sol.counts()["n_high"] > 0
 
 

@@ -54,7 +54,7 @@ def test_grid_unsorted_input_is_cell_multiset_equal():
 
 
 # --------------------------------------------------------------------------- step
-@pytest.mark.parametrize("fname", ["step_q1.npz", "step_q1_relax.npz"])
+@pytest.mark.parametrize("fname", ["step_q1.npz", "step_q1_relax.npz", "step_developed_51k.npz"])
 def test_step_matches_reference_fixture_bit_exact(fname):
     g = np.load(os.path.join(GOLDEN, fname))
     sc = scene_from_fixture(g)
@@ -298,3 +298,49 @@ def test_tether_guard_removes_the_zero_distance_nan():
             orc.step()
         finite[guard] = bool(np.isfinite(orc.get(1, "pos")).all())
     assert finite == {False: False, True: True}
+
+
+@pytest.mark.skipif(not O.refcpu_available(), reason="needs the reference checkout")
+def test_older_placement_matches_the_older_snapshots_own_code():
+    """TSS_FLAG_OLDER_PLACEMENT places each split's children exactly where the older
+    snapshot's initSubParticlesAndAddToList (TwoScale2D-master/TwoScale2D/
+    WCSPHSolver.cu:813-867, compiled here from the checkout) places them: at the
+    parent's predicted position +-DIR_LEN * r, with its predicted velocity."""
+    from twoscalesplit_gb300._abi import TSS_FLAG_OLDER_PLACEMENT
+    sc = scenes.dam_break_small(16, 32, seed=1, relax_iters=4)
+    sc.config.flags |= TSS_FLAG_OLDER_PLACEMENT
+    sc.config.roi[:] = [0.3, -math.inf, math.inf, math.inf]
+    o = O.Oracle(sc, 32)
+    checked = 0
+    for _ in range(60):
+        o.step()
+        split = o.get(0, "split")
+        if split.size == 0:
+            continue
+        lo, hi = o.state(0), o.state(1)
+        lpos = dict(zip(lo["id"].tolist(), lo["pos"].astype(np.float32)))
+        lvel = dict(zip(lo["id"].tolist(), lo["vel"].astype(np.float32)))
+        hix = {int(i): k for k, i in enumerate(hi["id"].tolist())}
+        for pid in split.tolist():
+            rp, rv = O.ref_older_children(np.float32(sc.config.r_low), pid, lpos[pid], lvel[pid])
+            for c in range(4):
+                k = hix[4 * pid + c]
+                assert np.array_equal(hi["pos"][k].astype(np.float32), rp[c]), (pid, c)
+                assert np.array_equal(hi["vel"][k].astype(np.float32), rv[c]), (pid, c)
+            checked += 1
+    assert checked > 0
+
+
+def test_relaxed_cfg0_runs_its_horizon():
+    """dam_break_5k with the older snapshot's placement and relaxation (4 x dt/10)
+    runs all its 2,000 steps finite, with the densities near rest density; with the
+    current tree's placement the same relaxation goes non-finite within 500 steps
+    (its first sub-step finds the children at 2-3 rest densities)."""
+    sc = scenes.dam_break_5k_relaxed(seed=0)
+    o = O.Oracle(sc, 32)
+    for _ in range(sc.steps):
+        o.step()
+    p0, p1 = o.state(0)["pos"], o.state(1)["pos"]
+    assert np.isfinite(p0).all() and np.isfinite(p1).all() and p1.shape[0] > 1000
+    d0, d1 = o.get(0, "dens"), o.get(1, "dens")
+    assert np.abs(d0 / 1000 - 1).mean() < 0.02 and np.abs(d1 / 1000 - 1).mean() < 0.1

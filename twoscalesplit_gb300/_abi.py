@@ -27,6 +27,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "CAPACI
 TSS_FLAG_Q1_COMPAT = 0x1
 TSS_FLAG_MERGE = 0x2
 TSS_FLAG_TETHER_GUARD = 0x4
+TSS_FLAG_OLDER_PLACEMENT = 0x8
 TSS_SCALE_LOW = 0
 TSS_SCALE_HIGH = 1
 

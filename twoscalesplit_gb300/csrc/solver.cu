@@ -338,6 +338,7 @@ Params make_params(const SceneIn& sc) {
     P.q1 = (cfg->flags & TSS_FLAG_Q1_COMPAT) ? 1 : 0;
     P.merge = (cfg->flags & TSS_FLAG_MERGE) ? 1 : 0;
     P.tether_guard = (cfg->flags & TSS_FLAG_TETHER_GUARD) ? 1 : 0;
+    P.older_place = (cfg->flags & TSS_FLAG_OLDER_PLACEMENT) ? 1 : 0;
     P.step0 = 0;
     P.Tle_r = sq_cutoff(P.r, true);
     P.Tlt_r = sq_cutoff(P.r, false);

@@ -15,8 +15,11 @@ namespace tss {
 __device__ __forceinline__ void make_children(const Params& P, const StepView& V, int i, int id, long long hb) {
     const float2 p = V.L.npos[i], v = V.L.nvel[i];
     const float rho = V.L.dens[i];
+    // the current tree's offset (initSubParticlesAndAddToList, WCSPHSolver.cu:956-1005)
+    // or the older snapshot's DIR_LEN * r (TwoScale2D-master/.../WCSPHSolver.cu:840-850)
     const float rad =
-        static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(2.0f * rho) * kPi)));
+        P.older_place ? 0.35355339f * P.r
+                      : static_cast<float>(0.5 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(2.0f * rho) * kPi)));
     const float2 cp[4] = {make_float2(p.x + rad, p.y + rad), make_float2(p.x - rad, p.y + rad),
                           make_float2(p.x + rad, p.y - rad), make_float2(p.x - rad, p.y - rad)};
 #pragma unroll

@@ -32,6 +32,7 @@ struct Params {
     int q1;
     int merge;             // TSS_FLAG_MERGE
     int tether_guard;      // TSS_FLAG_TETHER_GUARD
+    int older_place;       // TSS_FLAG_OLDER_PLACEMENT
     long long step0;       // the step counter when the scene started (its ROI's step 0)
     int slotsL, slotsH;    // slot-id spaces: low ids < slotsL, high ids < slotsH = 4*slotsL
     int capH;

@@ -83,36 +83,30 @@ def stage_bytes(stage, n_low, n_high, c_low, c_high, carry, n_fresh_children):
     return 0
 
 
-def measured_traffic(stage):
-    """DRAM bytes per launch of a stage's kernel from the committed ncu summary."""
+def _profile_value(fname, workload, arith, stage):
+    """A per-launch figure of a stage's kernel from a committed ncu summary table
+    (lines: workload arith stage value), or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+        with open(os.path.join(ROOT, "profiles", fname)) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) == 2 and not line.startswith("#") and parts[0] == stage:
-                    return float(parts[1])
+                if len(parts) == 4 and not line.startswith("#") and parts[:3] == [workload, arith, stage]:
+                    return float(parts[3])
     except OSError:
         pass
     return None
 
 
-def measured_warp_instructions(stage):
-    """Warp instructions per launch of a stage's kernel from the committed ncu summary."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "warp_instructions.txt")) as f:
-            for line in f:
-                parts = line.split()
-                if len(parts) == 2 and not line.startswith("#") and parts[0] == stage:
-                    return float(parts[1])
-    except OSError:
-        pass
-    return None
+def measured_traffic(workload, arith, stage):
+    """DRAM bytes per launch of a stage's kernel (profiles/dram_traffic.txt)."""
+    return _profile_value("dram_traffic.txt", workload, arith, stage)
 
 
-def issue_roofline(stage, launch_ms, sm_mhz):
-    """Instruction-issue roofline of a kernel: warp instructions per launch (ncu)
-    over its live launch time, against 4 warp instructions per SM per cycle."""
-    inst = measured_warp_instructions(stage)
+def issue_roofline(workload, arith, stage, launch_ms, sm_mhz):
+    """Instruction-issue roofline of a kernel: warp instructions per launch (ncu,
+    profiles/warp_instructions.txt) over its live launch time, against 4 warp
+    instructions per SM per cycle."""
+    inst = _profile_value("warp_instructions.txt", workload, arith, stage)
     if inst is None or not launch_ms or not sm_mhz:
         return None
     sms = 152
@@ -551,7 +545,7 @@ def run_ours(args):
     kind = "single" if start is None else "single_developed"
     K = args.steps
     legs = {}
-    for mode in ("exact", "fast"):
+    for mode in (("exact", "fast") if args.arith == "both" else (args.arith,)):
         sol.set_arith(mode)
         # warm-up (graph capture happens here), then the launch-shape autotuner on the
         # same state (its trial steps are warm-up too: the state is reset after them)
@@ -565,9 +559,8 @@ def run_ours(args):
         e2e_s, h2d, d2h = e2e_run(sol, sc, start, K, sh, world)
         legs[mode] = {"dev_ms": dev_ms, "wall": wall, "clk": clk, "stage": st_avg, "e2e_s": e2e_s, "h2d": h2d,
                       "d2h": d2h, "shape": shape, "tune_steps": tune_steps}
-        if args.exact_only:
-            break
-    sol.set_arith("exact")
+    head = "exact" if "exact" in legs else "fast"
+    sol.set_arith(head)
     # particles processed per step (deterministic replay of the exact steps, untimed)
     reset()
     counts = []
@@ -579,7 +572,7 @@ def run_ours(args):
     c_end = sol.counts()
     parts = float(sum(counts))
     splits_per_step = (c_end["total_split"] - c0["total_split"]) / K
-    times = torch.tensor([legs["exact"]["dev_ms"], legs["exact"]["e2e_s"], parts], dtype=torch.float64, device=dev)
+    times = torch.tensor([legs[head]["dev_ms"], legs[head]["e2e_s"], parts], dtype=torch.float64, device=dev)
     if world > 1:
         t_max = times.clone()
         torch.distributed.all_reduce(t_max[:2], op=torch.distributed.ReduceOp.MAX)
@@ -602,7 +595,7 @@ def run_ours(args):
     n_high_avg = float(np.mean(counts)) - sc.n_low
     carry = cfg.relax_iters > 0
 
-    def roofline(leg):
+    def roofline(leg, arith):
         st_avg = leg["stage"]
         top = max(st_avg, key=st_avg.get)
         top_bytes = stage_bytes(top, sc.n_low, n_high_avg, c_low, c_high, carry, 0)
@@ -611,7 +604,7 @@ def run_ours(args):
         step_bytes = sum(stage_bytes(s, sc.n_low, n_high_avg, c_low, c_high, carry, 0) for s in _abi.STAGE_NAMES)
         sv = survey_step_bytes(sc.n_low, n_high_avg, c_low, c_high, splits_per_step)
         return top, {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
-                     "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": measured_traffic(top),
+                     "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": measured_traffic(sc.name, arith, top),
                      "traffic_source": "profiles/dram_traffic.txt (ncu, one launch)",
                      "algorithmic_bytes_per_launch": top_bytes, "launch_ms": st_avg[top],
                      "step": {"algorithmic_bytes": step_bytes,
@@ -620,13 +613,14 @@ def run_ours(args):
                               "survey_model_bytes": sv,
                               "survey_model_frac": sv / (step_ms * 1e-3) / 1e9 / peak}}
 
-    ex = legs["exact"]
-    top, roof = roofline(ex)
+    ex = legs[head]
+    top, roof = roofline(ex, head)
     conf = workload_config(sc, start, args)
     conf.update({"n_high_end": c_end["n_high"], "splits_per_step": splits_per_step,
                  "l2": "flushed between timed steps (512 MiB write)", "parallelism": f"replicas{world}",
                  "launch": compact_shape(ex["shape"]), "autotune_steps": ex["tune_steps"],
-                 "arith": "exact (FP32, the reference's arithmetic; bit-identical to it)"})
+                 "arith": "exact (FP32, the reference's arithmetic; bit-identical to it)" if head == "exact" else
+                          "fast (TSS_ARITH_FAST, within 1e-5 of the reference per step)"})
     if start is not None:
         conf["develop_s"] = round(start["develop_s"], 2)
     line = {
@@ -634,7 +628,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ex["dev_ms"] / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": conf,
         "roofline": roof,
-        "issue_roofline": issue_roofline(top, ex["stage"][top], (ex["clk"] or {}).get("sm_mhz")),
+        "issue_roofline": issue_roofline(sc.name, head, top, ex["stage"][top], (ex["clk"] or {}).get("sm_mhz")),
         "stage_ms": {k: round(v, 5) for k, v in ex["stage"].items()},
         "e2e": {"value": parts_all / ex["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": ex["h2d"] / K,
                 "d2h_bytes_per_step": ex["d2h"] / K},
@@ -644,9 +638,9 @@ def run_ours(args):
         "clocks": ex["clk"],
         "wall_s_timed": ex["wall"],
     }
-    if "fast" in legs:
+    if head == "exact" and "fast" in legs:
         fa = legs["fast"]
-        ftop, froof = roofline(fa)
+        ftop, froof = roofline(fa, "fast")
         line["fast_arith"] = {
             "what": "TSS_ARITH_FAST: per pair an approximate rsqrt and reciprocal and FMAs; densities, forces and "
                     "positions within 1e-5 of the FP32 oracle per step (tests/test_gpu_fast_arith.py)",
@@ -654,7 +648,9 @@ def run_ours(args):
             "speedup_vs_exact": ex["dev_ms"] / fa["dev_ms"],
             "e2e": {"value": parts_all / fa["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": fa["h2d"] / K,
                     "d2h_bytes_per_step": fa["d2h"] / K},
-            "roofline": froof, "stage_ms": {k: round(v, 5) for k, v in fa["stage"].items()},
+            "roofline": froof,
+            "issue_roofline": issue_roofline(sc.name, "fast", ftop, fa["stage"][ftop], (fa["clk"] or {}).get("sm_mhz")),
+            "stage_ms": {k: round(v, 5) for k, v in fa["stage"].items()},
             "launch": compact_shape(fa["shape"]), "clocks": fa["clk"]}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, start, args.cpu_budget_s)
@@ -666,7 +662,9 @@ def run_ours(args):
 def run_batch(args):
     """The mixed-size batch workload: `--scenes` independent scenes advanced in
     lockstep by one batch (one grid build and one launch of each kernel per step),
-    against the same scenes advanced one at a time by the plain solver."""
+    against the same scenes advanced one at a time by the plain solver, in each
+    arithmetic of --arith (the plain solver in the same arithmetic as the batch:
+    the comparison is at the same tolerance)."""
     import torch
     from twoscalesplit_gb300 import _abi, build, scenes
     from twoscalesplit_gb300.solver import Batch, Solver
@@ -677,70 +675,81 @@ def run_batch(args):
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
-    b = Batch(scs)
-    init = b.download(0)
     empty = {"id": np.zeros(0, np.int32), "pos": np.zeros((0, 2), np.float32), "vel": np.zeros((0, 2), np.float32),
              "state": np.zeros(0, np.uint8)}
-    b.step(max(args.warmup, 1), stream=sh)
-    torch.cuda.synchronize(dev)
-    shape, tune_steps = tuned_shape(b, "batch", sum(sc.n_low for sc in scs), args)
-    b.upload(0, init)
-    b.upload(1, empty)
-    b.set_fresh(np.zeros(0, np.int32))
     K = args.steps
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    clocks = ClockSampler(None)
-    clocks.start()
-    for k in range(K):
-        flush.zero_()
-        evs[k][0].record(stream)
-        b.step(1, stream=sh)
-        evs[k][1].record(stream)
-    torch.cuda.synchronize(dev)
-    clk = clocks.stop()
-    b.sync()
-    batch_ms = sum(x.elapsed_time(y) for x, y in evs)
-    c = b.counts()
-    parts_end = c["n_low"] + c["n_high"]
-    # where a step's time goes once the high-res lists have filled: stage times
-    # (profiling graph) of 10 more steps from the final state, untimed above
-    b.profile(True)
-    st_sum = {k: 0.0 for k in _abi.STAGE_NAMES}
-    for _ in range(10):
-        flush.zero_()
-        b.step(1, stream=sh)
-        for name, v in b.stage_times().items():
-            st_sum[name] += v
-    b.profile(False)
-    del b
-    # the plain solver, one scene at a time, same steps
-    plain_ms = 0.0
-    n_plain = min(len(scs), args.plain_sample)
-    for sc in scs[:n_plain]:
-        sol = Solver.from_scene(sc)
-        sol.step(max(args.warmup, 1), stream=sh)
-        tuned_shape(sol, "single", sc.n_low, args)
-        torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sol.step(K, stream=sh)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        plain_ms += e0.elapsed_time(e1)
-        del sol
-    plain_ms *= len(scs) / n_plain
     n_low = sum(sc.n_low for sc in scs)
-    line = {"metric": "scene-steps/s", "value": len(scs) * K / (batch_ms / 1e3), "unit": "scene-steps/s",
-            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": batch_ms / K, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+    n_plain = min(len(scs), args.plain_sample)
+    legs = {}
+    for mode in (("exact", "fast") if args.arith == "both" else (args.arith,)):
+        suffix = "" if mode == "exact" else "_fast"
+        b = Batch(scs)
+        b.set_arith(mode)
+        init = b.download(0)
+        b.step(max(args.warmup, 1), stream=sh)
+        torch.cuda.synchronize(dev)
+        shape, tune_steps = tuned_shape(b, "batch" + suffix, n_low, args)
+        b.upload(0, init)
+        b.upload(1, empty)
+        b.set_fresh(np.zeros(0, np.int32))
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        clocks = ClockSampler(None)
+        clocks.start()
+        for k in range(K):
+            flush.zero_()
+            evs[k][0].record(stream)
+            b.step(1, stream=sh)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        clk = clocks.stop()
+        b.sync()
+        batch_ms = sum(x.elapsed_time(y) for x, y in evs)
+        c = b.counts()
+        # where a step's time goes once the high-res lists have filled: stage times
+        # (profiling graph) of 10 more steps from the final state, untimed above
+        b.profile(True)
+        st_sum = {k: 0.0 for k in _abi.STAGE_NAMES}
+        for _ in range(10):
+            flush.zero_()
+            b.step(1, stream=sh)
+            for name, v in b.stage_times().items():
+                st_sum[name] += v
+        b.profile(False)
+        del b
+        # the plain solver, one scene at a time, same steps, same arithmetic
+        plain_ms = 0.0
+        for sc in scs[:n_plain]:
+            sol = Solver.from_scene(sc)
+            sol.set_arith(mode)
+            sol.step(max(args.warmup, 1), stream=sh)
+            tuned_shape(sol, "single" + suffix, sc.n_low, args)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sol.step(K, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            plain_ms += e0.elapsed_time(e1)
+            del sol
+        plain_ms *= len(scs) / n_plain
+        legs[mode] = {"value": len(scs) * K / (batch_ms / 1e3), "ms_per_step": batch_ms / K,
+                      "particle_steps_per_s": n_low * K / (batch_ms / 1e3),
+                      "plain_one_at_a_time": {"scene_steps_per_s": len(scs) * K / (plain_ms / 1e3),
+                                              "sampled_scenes": n_plain, "ms_per_lockstep": plain_ms / K},
+                      "speedup_vs_plain": plain_ms / batch_ms, "clocks": clk,
+                      "n_high_end": c["n_high"], "n_particles_end": c["n_low"] + c["n_high"],
+                      "launch": compact_shape(shape), "autotune_steps": tune_steps,
+                      "stage_ms_end": {k: round(v / 10, 4) for k, v in st_sum.items()}}
+    head = legs["exact"] if "exact" in legs else legs["fast"]
+    line = {"metric": "scene-steps/s", "value": head["value"], "unit": "scene-steps/s",
+            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"mixed_batch_{len(scs)}", "scenes": len(scs), "n_low_total": n_low,
-                       "launch": compact_shape(shape), "autotune_steps": tune_steps,
-                       "n_high_end": c["n_high"], "l2": "flushed between timed steps (512 MiB write)"},
-            "particle_steps_per_s": n_low * K / (batch_ms / 1e3),
-            "plain_one_at_a_time": {"scene_steps_per_s": len(scs) * K / (plain_ms / 1e3),
-                                    "sampled_scenes": n_plain, "ms_per_lockstep": plain_ms / K},
-            "speedup_vs_plain": plain_ms / batch_ms, "clocks": clk, "n_particles_end": parts_end,
-            "stage_ms_end": {k: round(v / 10, 4) for k, v in st_sum.items()}}
+                       "arith": "exact" if "exact" in legs else "fast",
+                       "l2": "flushed between timed steps (512 MiB write)"},
+            **{k: v for k, v in head.items() if k not in ("value", "ms_per_step")}}
+    if "exact" in legs and "fast" in legs:
+        line["fast_arith"] = legs["fast"]
     print(json.dumps(line), flush=True)
 
 
@@ -769,8 +778,8 @@ def run_serve(args):
     if args.capacity_lps:
         cap_lps, cap_src = args.capacity_lps, "given on the command line"
     else:
-        cap_lps = measure_batch_capacity(dev)
-        cap_src = "mixed_batch_512, 10 steps after 3 warm-up steps"
+        cap_lps = measure_batch_capacity(dev, arith=args.arith)
+        cap_src = f"mixed_batch_512, 10 steps after 3 warm-up steps, {args.arith} arithmetic"
     # 2. the request stream
     rate = args.load * cap_lps / scenes.mean_work()
     trace = scenes.serving_trace(args.requests, rate, seed=args.seed)
@@ -779,7 +788,7 @@ def run_serve(args):
     walls = np.array([sc.n_wall for sc, _, _ in trace], dtype=np.float64)
     cfg = pool_config_for_budget(int(args.budget_gb * (1 << 30)), 1.25 * cells.sum() / n_low.sum() + 0.05,
                                  1.25 * walls.sum() / n_low.sum() + 0.05, max_scenes=8192)
-    sv = Server(cfg, max_steps_per_launch=args.chunk, max_in_flight=2, staging_bytes=2 << 30)
+    sv = Server(cfg, max_steps_per_launch=args.chunk, max_in_flight=2, staging_bytes=2 << 30, arith=args.arith)
     # warm-up: graph capture, first-touch of the staging rings
     warm = scenes.serving_trace(4, 1e3, seed=args.seed + 1, n_min=2000, n_max=20000, h_min=10, h_max=20)
     sv.run([Request(sc, h, t) for sc, h, t in warm])
@@ -796,6 +805,7 @@ def run_serve(args):
     # 3. the plain solver, one request at a time, each timed (create + steps + download)
     #    with the launch shape tuned for its size class; the classes are tuned first,
     #    on scratch solvers, so that no request takes trial steps
+    suffix = "" if args.arith == "exact" else "_fast"
     if not args.no_plain and not args.no_autotune:
         from twoscalesplit_gb300 import tuning
         seen = set()
@@ -803,16 +813,28 @@ def run_serve(args):
             cls = tuning.workload_class("single", sc.n_low)
             if cls not in seen:
                 seen.add(cls)
-                tuned_shape(Solver.from_scene(sc), "single", sc.n_low, args)
+                scratch = Solver.from_scene(sc)
+                scratch.set_arith(args.arith)
+                tuned_shape(scratch, "single" + suffix, sc.n_low, args)
     service = np.zeros(len(trace))
     exact = 0
     plain_steps_ms = 0.0
-    for k, (sc, h, _) in enumerate(trace if not args.no_plain else []):
+    # the requests the plain solver is timed on: all, or a seeded uniform sample of
+    # --plain-requests (a long stream's remaining service times are then estimated
+    # from the sample: service = a + b * n_low * horizon, least squares)
+    timed = list(range(len(trace)))
+    if args.plain_requests and args.plain_requests < len(trace):
+        timed = sorted(np.random.default_rng(args.seed + 7).choice(len(trace), args.plain_requests,
+                                                                   replace=False).tolist())
+        timed = sorted(set(timed) | set(verify))
+    for k in (timed if not args.no_plain else []):
+        sc, h, _ = trace[k]
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         sol = Solver.from_scene(sc)
+        sol.set_arith(args.arith)
         if not args.no_autotune:
-            tuned_shape(sol, "single", sc.n_low, args)  # from the cache: no steps
+            tuned_shape(sol, "single" + suffix, sc.n_low, args)  # from the cache: no steps
         sol.step(h)
         lo, hi = sol.download(0), sol.download(1)
         service[k] = time.perf_counter() - t0
@@ -828,6 +850,14 @@ def run_serve(args):
         del sol
     arrivals = np.array([t for _, _, t in trace])
     horizons = np.array([h for _, h, _ in trace], dtype=np.float64)
+    sampled = len(timed) < len(trace)
+    if sampled and not args.no_plain:
+        work = n_low * horizons
+        A = np.stack([np.ones(len(timed)), work[timed]], axis=1)
+        coef, *_ = np.linalg.lstsq(A, service[timed], rcond=None)
+        est = coef[0] + coef[1] * work
+        rest = np.setdiff1d(np.arange(len(trace)), timed)
+        service[rest] = est[rest]
     scene_steps = float(horizons[served].sum())
     makespan = summ["makespan_s"] - float(arrivals.min())
     plain_part, saturated = None, None
@@ -840,10 +870,27 @@ def run_serve(args):
             "latency_s": {"p50_s": float(np.percentile(plain_lat, 50)), "p99_s": float(np.percentile(plain_lat, 99)),
                           "mean_s": float(plain_lat.mean())},
             "service_s_total": float(service.sum()),
-            "how": "each request timed through the plain solver (create, horizon steps, download); FIFO "
-                   "completion times from those service times and the same arrivals"}
-        # 4. saturated: the first `burst` requests at once
+            "how": "computed, not replayed: each request timed alone through the plain solver (create, horizon "
+                   "steps, download), then FIFO completion times computed from those service times and the same "
+                   "arrivals" + (f"; {len(timed)} of the {len(trace)} requests timed (a seeded uniform sample), "
+                                 f"the others' service times estimated as a + b * n_low * horizon fitted to them "
+                                 f"(a = {coef[0]:.4f} s, b = {coef[1]:.3e} s)" if sampled else "")}
+        # 4. saturated: the first `burst` requests at once (all timed when sampled)
         nb = min(args.burst, len(trace))
+        if sampled:
+            for k in range(nb):
+                if k not in set(timed):
+                    sc, h, _ = trace[k]
+                    torch.cuda.synchronize(dev)
+                    t0 = time.perf_counter()
+                    sol = Solver.from_scene(sc)
+                    sol.set_arith(args.arith)
+                    if not args.no_autotune:
+                        tuned_shape(sol, "single" + suffix, sc.n_low, args)
+                    sol.step(h)
+                    sol.download(0), sol.download(1)
+                    service[k] = time.perf_counter() - t0
+                    del sol
         st_b, summ_b, _ = sv.run([Request(sc, h, 0.0) for sc, h, _ in trace[:nb]])
         burst_ss = float(sum(h for _, h, _ in trace[:nb]))
         saturated = {"requests": nb, "scene_steps_per_s": burst_ss / summ_b["makespan_s"],
@@ -862,7 +909,7 @@ def run_serve(args):
                        "pool": {"low_slots": cfg.low_slots, "high_particles": cfg.high_particles,
                                 "low_cells": cfg.low_cells, "high_cells": cfg.high_cells,
                                 "wall_particles": cfg.wall_particles},
-                       "max_steps_per_launch": args.chunk,
+                       "max_steps_per_launch": args.chunk, "arith": args.arith,
                        "l2": "inputs of the steps are the pool state (no flush; served end to end)"},
             "served": len(served), "rejected": int(sum(1 for st in stats if st["status"] == _abi.TSS_INVALID_ARG)),
             "latency_s": lat, "low_particle_steps_per_s": float(n_low[served] @ horizons[served]) / makespan,
@@ -872,7 +919,9 @@ def run_serve(args):
             "saturated": saturated,
             "exact_vs_alone": None if args.no_plain else f"{exact}/{len(verify)} requests bit-identical to the plain solver",
             "non_finite": {"served": numeric_served, "plain": None if args.no_plain else numeric_plain,
-                           "same_requests": None if args.no_plain else numeric_served == numeric_plain},
+                           "same_requests": None if args.no_plain else
+                           [k for k in numeric_served if k in set(timed)] == sorted(numeric_plain),
+                           "plain_checked": len(timed) if not args.no_plain else 0},
             "e2e": {"value": scene_steps / makespan, "unit": "scene-steps/s",
                     "h2d_bytes_per_step": float(sum(16 * sc.n_low + 8 * sc.n_wall for sc, _, _ in trace)) / max(summ["steps"], 1),
                     "d2h_bytes_per_step": float(sum(29 * 5 * sc.n_low for sc, _, _ in trace)) / max(summ["steps"], 1)},
@@ -880,13 +929,14 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_batch_capacity(dev, steps=10):
+def measure_batch_capacity(dev, steps=10, arith="exact"):
     """Low-res particle-steps/s of the batched step on the 512-scene mixed batch."""
     import torch
     from twoscalesplit_gb300 import scenes
     from twoscalesplit_gb300.solver import Batch
     scs = scenes.mixed_batch(512, seed=0)
     b = Batch(scs)
+    b.set_arith(arith)
     b.step(3)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -912,7 +962,7 @@ def run_serve_replicas(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     dist.init_process_group("gloo")
-    cap = args.capacity_lps or measure_batch_capacity(dev)
+    cap = args.capacity_lps or measure_batch_capacity(dev, arith=args.arith)
     cap = dispatch.gather(cap)[0]  # every replica uses rank 0's measurement
     rate = world * args.load * cap / scenes.mean_work()
     trace = scenes.serving_trace(args.requests * world, rate, seed=args.seed)
@@ -921,7 +971,7 @@ def run_serve_replicas(args, world, rank, local):
     walls = np.array([sc.n_wall for sc, _, _ in trace], dtype=np.float64)
     cfg = pool_config_for_budget(int(args.budget_gb * (1 << 30)), 1.25 * cells.sum() / n_low.sum() + 0.05,
                                  1.25 * walls.sum() / n_low.sum() + 0.05, max_scenes=8192)
-    sv = Server(cfg, max_steps_per_launch=args.chunk, max_in_flight=2, staging_bytes=2 << 30)
+    sv = Server(cfg, max_steps_per_launch=args.chunk, max_in_flight=2, staging_bytes=2 << 30, arith=args.arith)
     warm = scenes.serving_trace(4, 1e3, seed=args.seed + 1, n_min=2000, n_max=20000, h_min=10, h_max=20)
     sv.run([Request(sc, h, t) for sc, h, t in warm])
     reqs = [Request(sc, h, t) for sc, h, t in trace]
@@ -970,8 +1020,10 @@ def run_adaptive(args):
     build.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    sc = scenes.make_scene(args.scene if args.scene != "dam_break_1m" else "adaptive_8m", seed=0)
+    name = "adaptive_8m" if args.scene in ("dam_break_1m", "dam_break_1m_developed") else args.scene
+    sc = scenes.make_scene(name, seed=0)
     sol = Solver.from_scene(sc)
+    sol.set_arith(args.arith)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
@@ -1056,6 +1108,7 @@ def run_adaptive(args):
             "warmup": 0, "ms_per_step": dev_ms / max(done - len(checks), 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": sc.name, "n_low": n_low, "cap_high": sc.cap_high, "dt": float(sc.config.dt),
+                       "arith": args.arith,
                        "roi": list(sc.config.roi), "roi_velocity": list(sc.config.roi_velocity),
                        "flags": int(sc.config.flags), "check_every": every,
                        "l2": "inputs larger than L2 (8M-particle state)"},
@@ -1078,7 +1131,6 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scene", default="dam_break_1m_developed",
                     help="plain workload: dam_break_1m_developed (default), dam_break_1m or dam_break_5k")
-    ap.add_argument("--exact-only", action="store_true", help="plain workload: skip the fast-arithmetic leg")
     ap.add_argument("--start-cache", default=None,
                     help="plain workload: .npz of the developed start state (read if present, else written)")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
@@ -1095,11 +1147,19 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--capacity-lps", type=float, default=0.0)
     ap.add_argument("--no-plain", action="store_true", help="serve workload: skip the plain-solver comparison")
+    ap.add_argument("--plain-requests", type=int, default=0,
+                    help="serve workload: time the plain solver on this many sampled requests (0: all)")
+    ap.add_argument("--arith", default=None, choices=["exact", "fast", "both"],
+                    help="the gathers' arithmetic (plain and batch default: both; serve, adaptive: exact)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape of the gathers")
     ap.add_argument("--launch-cache", default=None, help="launch-shape cache file (default: the user cache)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"plain": 500, "batch": 1000, "adaptive": 2000}.get(args.workload, 200)
+    if args.arith is None:
+        args.arith = "both" if args.workload in ("batch", "plain") else "exact"
+    if args.arith == "both" and args.workload in ("serve", "adaptive"):
+        sys.exit("--arith both is for the batch workload")
     if args.workload == "batch":
         run_batch(args)
     elif args.workload == "serve":

@@ -287,6 +287,9 @@ typedef struct tss_serve_summary {
 } tss_serve_summary;
 
 tss_status tss_server_create(const tss_server_config* cfg, tss_server** out);
+/* The arithmetic of the server pool's gathers (tss_solver_set_arith on its pool;
+ * TSS_ARITH_EXACT by default).  Call between runs. */
+tss_status tss_server_set_arith(tss_server* sv, int mode);
 tss_status tss_server_run(tss_server* sv, int n, const tss_request* reqs, tss_request_stats* stats,
                           tss_serve_summary* summary);
 void tss_server_destroy(tss_server* sv);

@@ -142,6 +142,14 @@ public:
     }
     tss_solver* handle() { return mS; }
 
+    // The gathers' arithmetic (tss_solver_set_arith; not in the reference): false
+    // (the default) keeps the reference's FP32 arithmetic bit for bit, true spends
+    // the step's 1e-5 tolerance on approximate square roots and reciprocals.
+    void SetFastArithmetic(bool on) {
+        if (!mS) Bind();
+        throw_on(tss_solver_set_arith(mS, on ? TSS_ARITH_FAST : TSS_ARITH_EXACT), mS);
+    }
+
     // Launch-shape autotuner (tss_solver_autotune; not in the reference): times the
     // candidate shapes on this solver's own steps, which advance its state, and
     // installs the fastest per gather.

@@ -4,8 +4,8 @@
                          OpenMP, -ffp-contract=off so FP32 follows the reference's
                          operation order without fused multiply-adds)
   _ref/librefcpu.so   -- the reference's own kernel source compiled for the CPU
-                         (refcpu/build_ref.sh); only when the reference checkout is
-                         present, i.e. on the build machine, not on the GPU machine
+                         (refcpu/build_ref.sh); only when a reference checkout is
+                         given, i.e. on the build machine, not on the GPU machine
   _ref/refkern.cubin  -- the reference's own kernel source compiled for sm_103a
                          (refgpu/build_refgpu.sh); only where the checkout is
                          present.  Device code only: it travels to the GPU machine.
@@ -22,7 +22,17 @@ ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REFCPU_SO = os.path.join(HERE, "_ref", "librefcpu.so")
 REFGPU_CUBIN = os.path.join(HERE, "_ref", "refkern.cubin")
 REFGPU_SO = os.path.join(HERE, "librefgpu.so")
-REFERENCE_ROOT = os.environ.get("TSS_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root(root=None):
+    """The reference checkout to build from: `root`, else $TSS_REFERENCE_ROOT, else
+    None (then only the prebuilt files are used)."""
+    root = root or os.environ.get("TSS_REFERENCE_ROOT")
+    if root and os.path.exists(os.path.join(root, "TwoScale2D", "WCSPHSolver.cu")):
+        return root
+    if root:
+        sys.stderr.write(f"oracle: no reference sources under {root}; using the prebuilt files if any\n")
+    return None
 
 
 def _stale(target, sources):
@@ -43,28 +53,30 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def build_refcpu(force=False):
-    """Returns the library path, or None when the reference sources are absent."""
-    cur = os.path.join(REFERENCE_ROOT, "TwoScale2D", "WCSPHSolver.cu")
-    if not os.path.exists(cur):
-        return None
+def build_refcpu(force=False, root=None):
+    """Returns the library path: built from the reference checkout (`root` or
+    $TSS_REFERENCE_ROOT) when given, else the prebuilt library if any, else None."""
+    ref = reference_root(root)
+    if ref is None:
+        return REFCPU_SO if os.path.exists(REFCPU_SO) else None
     deps = [os.path.join(HERE, "refcpu", f) for f in ("cuda_shim.h", "refcpu_harness.inc", "build_ref.sh")]
     if not force and not _stale(REFCPU_SO, deps):
         return REFCPU_SO
-    subprocess.check_call(["sh", os.path.join(HERE, "refcpu", "build_ref.sh"), REFERENCE_ROOT])
+    subprocess.check_call(["sh", os.path.join(HERE, "refcpu", "build_ref.sh"), ref])
     return REFCPU_SO
 
 
-def build_refgpu_cubin(force=False):
-    """Returns the cubin path, or None when the reference sources are absent (the
-    cubin built on the build machine is then used if it is there)."""
-    cur = os.path.join(REFERENCE_ROOT, "TwoScale2D", "WCSPHSolver.cu")
-    if not os.path.exists(cur):
+def build_refgpu_cubin(force=False, root=None):
+    """Returns the cubin path: built from the reference checkout (`root` or
+    $TSS_REFERENCE_ROOT) when given, else the cubin built on the build machine if it
+    is there, else None."""
+    ref = reference_root(root)
+    if ref is None:
         return REFGPU_CUBIN if os.path.exists(REFGPU_CUBIN) else None
     deps = [os.path.join(HERE, "refgpu", f) for f in ("refgpu_shim.cuh", "refgpu_entry.inc", "build_refgpu.sh")]
     if not force and not _stale(REFGPU_CUBIN, deps):
         return REFGPU_CUBIN
-    subprocess.check_call(["sh", os.path.join(HERE, "refgpu", "build_refgpu.sh"), REFERENCE_ROOT])
+    subprocess.check_call(["sh", os.path.join(HERE, "refgpu", "build_refgpu.sh"), ref])
     return REFGPU_CUBIN
 
 
@@ -84,12 +96,16 @@ def build_refgpu_launcher(force=False):
     return REFGPU_SO
 
 
-def build(force=False):
+def build(force=False, root=None):
     build_oracle(force)
-    build_refcpu(force)
-    build_refgpu_cubin(force)
+    if reference_root(root) is None:
+        sys.stderr.write("oracle: no reference checkout given (pass it, or set TSS_REFERENCE_ROOT): the "
+                         "reference's kernels are not rebuilt\n")
+    build_refcpu(force, root)
+    build_refgpu_cubin(force, root)
     build_refgpu_launcher(force)
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    build(force="--force" in sys.argv, root=args[0] if args else None)

@@ -5,9 +5,10 @@
 # 14-1747 in namespace `older`, for the relaxation kernels) compiled for the CPU
 # with cuda_shim.h and driven by refcpu_harness.inc.  The source is streamed from
 # the reference checkout into the compiler; nothing of it is written to disk.
-# Usage: build_ref.sh [REFERENCE_ROOT]
+# Usage: build_ref.sh REFERENCE_ROOT   (the directory holding the reference checkout)
 set -e
-REF=${1:-/root/reference}
+[ -n "$1" ] || { echo "usage: $0 REFERENCE_ROOT (the reference checkout)" >&2; exit 2; }
+REF=$1
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"
 CUR="$REF/TwoScale2D/WCSPHSolver.cu"

@@ -6,9 +6,10 @@
 # refgpu_entry.inc.  The source is streamed from the reference checkout into nvcc;
 # nothing of it is written to disk.  The cubin is device code only, so it runs on
 # any host: refgpu_launcher.cu loads it with the driver API.
-# Usage: build_refgpu.sh [REFERENCE_ROOT]
+# Usage: build_refgpu.sh REFERENCE_ROOT   (the directory holding the reference checkout)
 set -e
-REF=${1:-/root/reference}
+[ -n "$1" ] || { echo "usage: $0 REFERENCE_ROOT (the reference checkout)" >&2; exit 2; }
+REF=$1
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"
 CUR="$REF/TwoScale2D/WCSPHSolver.cu"

@@ -21,8 +21,8 @@ from the reference checkout by oracle/refcpu/build_ref.sh) and run headless:
                       kernels on this schedule, tests/test_oracle_cpu.py) and the
                       recorded step is the reference's own
 
-Run from the repository root on a machine with the reference checkout:
-    python tests/golden/make_golden.py
+Run from the repository root with the reference checkout named:
+    TSS_REFERENCE_ROOT=<checkout> python tests/golden/make_golden.py
 """
 import math
 import os

@@ -292,6 +292,7 @@ def load_library(path=None):
         "tss_server_run": (i, [vp, i, ctypes.POINTER(TssRequest), ctypes.POINTER(TssRequestStats),
                                ctypes.POINTER(TssServeSummary)]),
         "tss_server_destroy": (None, [vp]),
+        "tss_server_set_arith": (i, [vp, i]),
         "tss_server_last_error": (i, [vp, ctypes.c_char_p, i]),
         "tss_render_workspace_size": (i, [i, ctypes.POINTER(TssView), f, ctypes.POINTER(ctypes.c_size_t)]),
         "tss_render_clear": (i, [vp, i, i, vp]),

@@ -330,6 +330,11 @@ struct Run {
 
 extern "C" {
 
+tss_status tss_server_set_arith(tss_server* sv, int mode) {
+    if (!sv) return TSS_INVALID_ARG;
+    return tss_solver_set_arith(sv->pool, mode);
+}
+
 tss_status tss_server_create(const tss_server_config* cfg, tss_server** out) {
     if (!cfg || !out || cfg->max_steps_per_launch < 1 || cfg->max_in_flight < 1 || cfg->staging_bytes < (1 << 20))
         return TSS_INVALID_ARG;

@@ -158,7 +158,7 @@ class Request:
 class Server:
     """The library's serving loop (tss_server_*) over a pool of `cfg`."""
 
-    def __init__(self, cfg, max_steps_per_launch=8, max_in_flight=2, staging_bytes=1 << 30):
+    def __init__(self, cfg, max_steps_per_launch=8, max_in_flight=2, staging_bytes=1 << 30, arith="exact"):
         self.lib = load_library()
         sc = _abi.TssServerConfig()
         sc.pool = cfg
@@ -168,6 +168,9 @@ class Server:
         h = ctypes.c_void_p()
         check(self.lib.tss_server_create(ctypes.byref(sc), ctypes.byref(h)))
         self.h = h
+        if arith not in ("exact", "fast"):
+            raise ValueError("arith must be 'exact' or 'fast'")
+        check(self.lib.tss_server_set_arith(h, _abi.TSS_ARITH_FAST if arith == "fast" else _abi.TSS_ARITH_EXACT))
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:

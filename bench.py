@@ -52,6 +52,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s"
+GATHER_STAGES = ("density_high", "density_low", "force_low", "force_high")
 UNIT = "particle-steps/s"
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
@@ -61,15 +62,15 @@ FALLBACK_HBM_GBS = 6800.0
 # algorithmic bytes (compulsory own-state traffic per particle; neighbour gathers
 # are served on chip).  Per-particle and per-cell figures per stage.
 # ---------------------------------------------------------------------------
-def stage_bytes(stage, n_low, n_high, c_low, c_high, carry, n_fresh_children):
+def stage_bytes(stage, n_low, n_high, c_low, c_high, carry, n_fresh_children, relax_iters=0):
     cg = 16 if carry else 0
     grid = lambda n, c: n * (16 + 24 + 45 + cg) + 12 * c  # keys, scatter, reorder; scan 12 B/cell
     if stage == "grid_high":
         return grid(n_high, c_high)
     if stage == "grid_low":
         return grid(n_low, c_low)
-    if stage == "relax":
-        return n_fresh_children * 4 * (8 + 8 + 8 + 8 + 16)  # per iteration: R pos,vel,dens/pres; W pos,vel...
+    if stage == "relax":  # per sub-step, per child: R pos, vel (16); W dens, pres (8); W pos, vel twice (32)
+        return n_fresh_children * relax_iters * 56
     if stage == "density_high":
         return n_high * 21 + 4 * c_high
     if stage == "density_low":
@@ -595,13 +596,18 @@ def run_ours(args):
     n_high_avg = float(np.mean(counts)) - sc.n_low
     carry = cfg.relax_iters > 0
 
+    n_fresh = 4.0 * splits_per_step  # children relaxed per step
+
     def roofline(leg, arith):
         st_avg = leg["stage"]
-        top = max(st_avg, key=st_avg.get)
-        top_bytes = stage_bytes(top, sc.n_low, n_high_avg, c_low, c_high, carry, 0)
+        # the dominant single kernel: the gathers (a grid build or a relaxation
+        # sub-step is several launches)
+        top = max(GATHER_STAGES, key=lambda k: st_avg[k])
+        top_bytes = stage_bytes(top, sc.n_low, n_high_avg, c_low, c_high, carry, n_fresh, cfg.relax_iters)
         top_gbs = top_bytes / (st_avg[top] * 1e-3) / 1e9 if st_avg[top] > 0 else 0.0
         step_ms = leg["dev_ms"] / K
-        step_bytes = sum(stage_bytes(s, sc.n_low, n_high_avg, c_low, c_high, carry, 0) for s in _abi.STAGE_NAMES)
+        step_bytes = sum(stage_bytes(s, sc.n_low, n_high_avg, c_low, c_high, carry, n_fresh, cfg.relax_iters)
+                         for s in _abi.STAGE_NAMES)
         sv = survey_step_bytes(sc.n_low, n_high_avg, c_low, c_high, splits_per_step)
         return top, {"bound": "hbm", "kernel": top, "achieved": top_gbs, "peak": peak, "unit": "GB/s",
                      "frac": top_gbs / peak, "peak_source": peak_kind, "traffic": measured_traffic(sc.name, arith, top),

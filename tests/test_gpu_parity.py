@@ -295,6 +295,36 @@ def test_1m_dam_break_one_step_parity_and_invariants():
     assert m * np.float32((d["state"] == 0).sum()) + mh * np.float32(c["n_high"]) == m * np.float32(sc.n_low)
 
 
+def test_1m_developed_multistep_parity():
+    """The 1M dam break once its front carries parents through the region of interest
+    (20,000 steps on the GPU, ~400k high-res particles, tens of splits per step):
+    three more steps bit-exact against the FP32 oracle started from the same state --
+    sorted ids, cell offsets, densities, pressures, accelerations, split sets, both
+    lists after each step."""
+    sc = scenes.dam_break_1m(seed=0)
+    sc.config.flags |= _abi.TSS_FLAG_TETHER_GUARD
+    sol = Solver.from_scene(sc)
+    sol.step(20000)
+    sol.sync()
+    orc = O.Oracle(sc, 32)
+    for s in (TSS_SCALE_LOW, TSS_SCALE_HIGH):
+        d = sol.download(s)
+        orc.set_scale(s, d["id"], d["pos"], d["vel"], d["state"], d["dens"], d["pres"])
+    orc.set_fresh(sol.get_fresh())
+    orc.set_steps(sol.counts()["steps"])
+    assert sol.counts()["n_high"] > 100_000
+    splits = 0
+    for k in range(3):
+        sol.step(1)
+        sol.sync()
+        orc.step()
+        _compare_step_buffers(sol, orc, k)
+        _assert_state_equal(sol, orc, TSS_SCALE_LOW, k)
+        _assert_state_equal(sol, orc, TSS_SCALE_HIGH, k)
+        splits += sol.copy(TSS_SCALE_LOW, _abi.TSS_BUF_SPLIT).shape[0]
+    assert splits > 0
+
+
 def test_determinism_bitwise():
     sc = scenes.dam_break_5k(seed=9)
     a, b = Solver.from_scene(sc), Solver.from_scene(sc)

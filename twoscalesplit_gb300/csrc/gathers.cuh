@@ -53,7 +53,7 @@ using namespace gather_detail;
 // High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
 // ---------------------------------------------------------------------------
 template <class A, class G>
-__device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i) {
+__device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i, bool hstate0) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     const int* offH = H.off + P.cbH;
@@ -76,7 +76,13 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
         term, add_density, d);
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    if (P.q1) {
+    // With no high-res entry in state 0 in this step (hstate0 false), a state-1
+    // particle's Q1 term can take only never-created slots (position (0,0), state 0:
+    // lambda_HL rejects every existing state-1 entry), and those only when the
+    // particle lies within r_h of (0,0): otherwise the walk adds nothing and is
+    // skipped -- the same terms, none.
+    const bool q1_live = hstate0 || (s & 1u) == 0u || sq(p) <= P.Tle_rh;
+    if (P.q1 && q1_live) {
         // The reference reads the HIGH sorted list at LOW-grid ranges of its own
         // scene; past the scene's n_high that list still holds its initial identity
         // (slot t at position t).  A row's range [a, b) of low-list positions t
@@ -117,7 +123,7 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
                 },
                 term, add_density, d);
         }
-    } else {
+    } else if (!P.q1) {
         G::window(
             offL, P.dimL[0], csx, cex, csy, cey,
             [&](int k) {
@@ -141,12 +147,13 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
 
 template <bool B, class G, class A>
 __global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
+    const bool hstate0 = V.cnt->h_state0 != 0;
     for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];
-            density_high_one<A, G>(P, V, i);
+            density_high_one<A, G>(P, V, i, hstate0);
         } else {
-            density_high_one<A, G>(P0, V, i);
+            density_high_one<A, G>(P0, V, i, hstate0);
         }
     });
 }
@@ -323,6 +330,13 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     if (G::leader()) {
         L.acc[i] = acc;
         if (!isfinite(acc.x) || !isfinite(acc.y)) atomicOr(&V.cnt->err, kErrNumeric);
+        // a split parent's tether radius, 0.75 sqrt(m / (rho pi)) in double as the
+        // reference evaluates it (adjustPosition, WCSPHSolver.cu:1007-1022), once per
+        // parent here instead of once per child in the high-res force: FP64 is slow
+        // on this GPU.  min(dist, float(R)) == float(min(dist, R)) for a float dist
+        // (rounding is monotone), so the children's clamp is unchanged bit for bit.
+        if (s == 1u)
+            L.tr[i] = static_cast<float>(0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(dens) * kPi)));
         L.npos[i] = p;
         L.nvel[i] = v;
         L.nid[i] = L.id[i];
@@ -446,11 +460,9 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
         drop = P.merge && pi >= 0 && L.st[pi] == 1 && L.nst[pi] == 0;
         if (pi >= 0 && L.st[pi] == 1 && !drop) {
             const float2 pl = L.npos[pi];
-            const float rho = L.dens[pi];
             const float2 pji = sub(p, pl);
             const float dist = vnorm(pji);
-            const float lim = static_cast<float>(fmin(
-                static_cast<double>(dist), 0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(rho) * kPi))));
+            const float lim = fminf(dist, L.tr[pi]);  // the parent's radius, from the low-res force
             if (!(P.tether_guard && dist == 0.0f)) {  // guarded: a child on its parent stays there
                 p.x = pl.x + lim / dist * pji.x;
                 p.y = pl.y + lim / dist * pji.y;

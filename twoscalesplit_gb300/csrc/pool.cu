@@ -213,6 +213,7 @@ void plan_pool(tss_solver* s, const tss_pool_config& c, Arena& A, PoolPlan& pp) 
         A.add(&b.dens, cap);
         A.add(&b.pres, cap);
         A.add(&b.q, cap);
+        A.add(&b.tr, cap);
         A.add(&b.ndens, s->carry ? cap : 1);
         A.add(&b.npres, s->carry ? cap : 1);
     };

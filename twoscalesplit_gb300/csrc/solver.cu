@@ -25,6 +25,7 @@ StepView tss_solver::view() const {
         s.dens = b.dens;
         s.pres = b.pres;
         s.q = b.q;
+        s.tr = b.tr;
         s.acc = b.acc;
         s.off = b.g.off;
         s.map = b.map;
@@ -472,6 +473,7 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
         A.add(&b.dens, cap);
         A.add(&b.pres, cap);
         A.add(&b.q, cap);
+        A.add(&b.tr, cap);
         A.add(&b.ndens, s->carry ? cap : 1);
         A.add(&b.npres, s->carry ? cap : 1);
     };

@@ -31,6 +31,7 @@ struct ScaleBufs {
     uint8_t *st, *nst;
     int32_t *id, *nid, *map;
     float *dens, *pres, *q, *ndens, *npres;
+    float* tr;  // low scale: a split parent's tether radius this step (sorted order)
     GridBufs g;
 };
 

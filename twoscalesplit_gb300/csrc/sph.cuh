@@ -16,6 +16,7 @@ struct ScaleView {
     float* dens;
     float* pres;
     float* q;        // p / rho^2
+    float* tr;       // low scale: each split parent's tether radius, written by the low-res force
     float2* acc;
     const int* off;  // dense cell offsets [C+1]
     int32_t* map;    // slot id -> index in the cur arrays

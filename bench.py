@@ -903,7 +903,9 @@ def run_serve(args):
                      "plain_scene_steps_per_s": burst_ss / float(service[:nb].sum()),
                      "speedup_vs_plain": float(service[:nb].sum()) / summ_b["makespan_s"],
                      "mean_active_scenes": summ_b["mean_active"]}
-    gpu_launches = int(summ["steps"] * 14 + len(served) * 16)
+    # kernels: 12 per pool step; per request about 11 at admission (keys, slot-map
+    # fill, wall grid build, counters), 2 at extraction and 4 at retirement
+    gpu_launches = int(summ["steps"] * 12 + len(served) * 17)
     line = {"metric": "scene-steps/s", "value": scene_steps / makespan, "unit": "scene-steps/s", "n_gpus": 1,
             "steps": int(summ["steps"]), "warmup": 1, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -1006,7 +1008,7 @@ def run_serve_replicas(args, world, rank, local):
                         "h2d_bytes_per_step": float(sum(16 * sc.n_low + 8 * sc.n_wall for sc, _, _ in trace))
                         / max(summ["steps"], 1),
                         "d2h_bytes_per_step": float(sum(29 * 5 * sc.n_low for sc, _, _ in trace)) / max(summ["steps"], 1)},
-                "gpu_launches": int(summ["steps"] * 14 + len(served) * 16), "clocks": clk}
+                "gpu_launches": int(summ["steps"] * 12 + len(served) * 17), "clocks": clk}
         print(json.dumps(line), flush=True)
     dist.destroy_process_group()
 
@@ -1124,7 +1126,7 @@ def run_adaptive(args):
                             "acc_err_max_over_rms": acc_rms, "acc_err_max_over_g": acc_g,
                             "checks": len(checks),
                             "tolerance": "dens 1e-5 relative"},
-            "checks": checks, "clocks": clk, "gpu_launches": done * 14}
+            "checks": checks, "clocks": clk, "gpu_launches": done * 12}
     print(json.dumps(line), flush=True)
 
 

@@ -356,11 +356,14 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
 // trips, lanes past n inactive) so the ballot that feeds the split compaction sees
 // whole warps; a warp's 32 particles lie in one compaction tile (kSplitTile % 32 ==
 // 0).  One particle per warp: the leader counts its particle's split.
-// 48 registers (five blocks per SM) in both forms.  The batched form measured the
-// same at 40 and 48 on a batch of 512 mixed scenes (4.11 / 4.08 ms), 3-7 % faster
-// at 48 on batches of one scene, and 10 % slower at 64.
+// 48 registers (five blocks per SM) in both forms of the exact arithmetic.  The
+// batched form measured the same at 40 and 48 on a batch of 512 mixed scenes (4.11
+// / 4.08 ms), 3-7 % faster at 48 on batches of one scene, and 10 % slower at 64.
+// The single-scene form in the tolerance arithmetic fits 40 registers without
+// spilling and runs six blocks per SM: 3.5 % faster on the developed 1M dam break
+// (0.130 -> 0.125 ms); batched, it would spill 76 bytes at 40 and keeps 48.
 template <bool B, class G, class A>
-__global__ void __launch_bounds__(256, 5) k_force_low(Params P0, StepView V) {
+__global__ void __launch_bounds__(256, (A::kFast && !B) ? 6 : 5) k_force_low(Params P0, StepView V) {
     const int n = V.cnt->cur[0];
     const bool cross = V.cnt->h_state0 != 0;
     const auto one = [&](int i) {
@@ -494,9 +497,11 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
 // third of that, at 64 (four blocks per SM) nothing -- as fast as 48 on a batch of
 // 512 mixed scenes and 15 % faster on a batch of one 162k-particle scene.  The
 // single-scene form at 48 registers (five blocks) spills 64 bytes instead of 120
-// at 40 and measured 3-4 % faster.
+// at 40 and measured 3-4 % faster.  In the tolerance arithmetic the single-scene
+// form needs no spill at 40 registers (six blocks per SM) and is 3.8 % faster there
+// on the developed 1M dam break (0.159 -> 0.153 ms).
 template <bool B, class G, class A>
-__global__ void __launch_bounds__(256, B ? 4 : 5) k_force_high(Params P0, StepView V) {
+__global__ void __launch_bounds__(256, B ? 4 : (A::kFast ? 6 : 5)) k_force_high(Params P0, StepView V) {
     for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];

@@ -49,6 +49,51 @@ __device__ __forceinline__ void for_each_particle(int n, F&& f) {
 }  // namespace gather_detail
 using namespace gather_detail;
 
+// Neighbour lists (ScaleView::nbr).  A density pass that runs one particle per
+// thread records the same-scale candidates its window accepts, in window order,
+// and the force pass of the same step walks that list instead of its window: the
+// force's own candidates are a subset of the density's (same positions and
+// states, cutoff d < r and d != 0 against d <= r, the same lambda masks), so
+// testing each listed candidate again with the force's test gives the force's
+// candidates in the same order -- the same sums, bit for bit -- without scanning
+// the ~36 candidates of the window, of which about a third are accepted.  A
+// particle with more than kMaxNbr neighbours, or one whose offset does not fit
+// 16 bits, is marked and walks its window.
+struct NbrRecord {
+    int16_t* nbr;
+    int stride, i, n;
+    bool ok;
+    __device__ __forceinline__ NbrRecord(const ScaleView& S, int i_)
+        : nbr(S.nbr), stride(S.nbr_stride), i(i_), n(0), ok(true) {}
+    __device__ __forceinline__ void add(int j) {
+        if (j == i) return;  // the density's self term: never a force pair
+        const int dj = j - i;
+        if (n < kMaxNbr && dj >= -32768 && dj <= 32767) nbr[n * stride + i] = static_cast<int16_t>(dj);
+        else ok = false;
+        ++n;
+    }
+    __device__ __forceinline__ void finish(const ScaleView& S) const {
+        S.nnbr[i] = ok ? static_cast<uint8_t>(n) : kNbrOverflow;
+    }
+};
+
+// The force pass's same-scale pairs: from the list when there is one, else `walk`.
+template <class G, class T, class Test, class Term, class Add, class Walk>
+__device__ __forceinline__ void list_or_walk(const ScaleView& S, int i, Test&& test, Term&& term, Add&& add,
+                                             T& sum, Walk&& walk) {
+    if constexpr (!G::kWarp) {
+        const int nc = S.nbr ? S.nnbr[i] : kNbrOverflow;
+        if (nc != kNbrOverflow) {
+            for (int c = 0; c < nc; ++c) {
+                const int k = i + S.nbr[c * S.nbr_stride + i];
+                if (test(k)) add(sum, term(k));
+            }
+            return;
+        }
+    }
+    walk();
+}
+
 // ---------------------------------------------------------------------------
 // High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
 // ---------------------------------------------------------------------------
@@ -63,6 +108,8 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
     float d = 0.0f, dl = 0.0f;
     float x = 0.0f;
     const auto term = [&](int) { return A::density(P, x); };
+    const bool rec_on = !G::kWarp && H.nbr != nullptr;
+    NbrRecord rec(H, i);
     int csx, csy, cex, cey;
     grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
     grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
@@ -73,7 +120,12 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
             x = sq(sub(p, H.pos[k]));
             return x <= P.Tle_rh;
         },
-        term, add_density, d);
+        [&](int j) {
+            if (rec_on) rec.add(j);
+            return A::density(P, x);
+        },
+        add_density, d);
+    if (rec_on) rec.finish(H);
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     // With no high-res entry in state 0 in this step (hstate0 false), a state-1
@@ -170,6 +222,8 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
     float d = 0.0f, dh = 0.0f;
     float x = 0.0f;
     const auto term = [&](int) { return A::density(P, x); };
+    const bool rec_on = !G::kWarp && L.nbr != nullptr;
+    NbrRecord rec(L, i);
     int csx, csy, cex, cey;
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
@@ -179,7 +233,12 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
             x = sq(sub(p, L.pos[k]));
             return x <= P.Tle_r;
         },
-        term, add_density, d);
+        [&](int j) {
+            if (rec_on) rec.add(j);
+            return A::density(P, x);
+        },
+        add_density, d);
+    if (rec_on) rec.finish(L);
     if (cross) {  // only state-0 high-res particles can contribute (lambda_LH)
         grid_coord_s<1>(P, p.x, p.y, -P.r, csx, csy);
         grid_coord_s<1>(P, p.x, p.y, P.r, cex, cey);
@@ -268,15 +327,18 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
     int csx, csy, cex, cey;
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    G::window(
-        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
-        [&](int k) {
+    {
+        const auto test = [&](int k) {
             pij = sub(p, L.pos[k]);
             x = sq(pij);
             return x != 0.0f && x <= P.Tlt_r && notDeleted(L.st[k]);
-        },
-        [&](int j) { return A::template pair<kHLow>(P, pij, x, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j]); },
-        add_terms, fl);
+        };
+        const auto term = [&](int j) {
+            return A::template pair<kHLow>(P, pij, x, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j]);
+        };
+        list_or_walk<G>(L, i, test, term, add_terms, fl,
+                        [&] { G::window(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey, test, term, add_terms, fl); });
+    }
     const float2 accB = wall_sum<A, G, 0>(P, V, p, csx, cex, csy, cey, P.Tle_r, P.cBL);
     PairTerms fh{make_float2(0.f, 0.f), fl.t};  // (accH, accT): the sigma sum continues
     if (cross) {
@@ -408,16 +470,19 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     int csx, csy, cex, cey;
     grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
     grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
-    G::window(
-        H.off + P.cbH, P.dimH[0], csx, cex, csy, cey,
-        [&](int k) {
+    {
+        const auto test = [&](int k) {
             if (!lamHH(s, H.st[k])) return false;
             pij = sub(p, H.pos[k]);
             x = sq(pij);
             return x != 0.0f && x <= P.Tlt_rh;
-        },
-        [&](int j) { return A::template pair<kHHigh>(P, pij, x, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j]); },
-        add_terms, fh);
+        };
+        const auto term = [&](int j) {
+            return A::template pair<kHHigh>(P, pij, x, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j]);
+        };
+        list_or_walk<G>(H, i, test, term, add_terms, fh,
+                        [&] { G::window(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey, test, term, add_terms, fh); });
+    }
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     PairTerms fl{make_float2(0.f, 0.f), fh.t};  // (accL, accT): the sigma sum continues

@@ -214,6 +214,9 @@ void plan_pool(tss_solver* s, const tss_pool_config& c, Arena& A, PoolPlan& pp) 
         A.add(&b.pres, cap);
         A.add(&b.q, cap);
         A.add(&b.tr, cap);
+        A.add(&b.nbr, static_cast<size_t>(kMaxNbr) * (cap > 0 ? cap : 1));
+        A.add(&b.nnbr, cap);
+        b.cap = cap > 0 ? cap : 1;
         A.add(&b.ndens, s->carry ? cap : 1);
         A.add(&b.npres, s->carry ? cap : 1);
     };

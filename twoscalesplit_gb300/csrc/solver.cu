@@ -26,6 +26,9 @@ StepView tss_solver::view() const {
         s.pres = b.pres;
         s.q = b.q;
         s.tr = b.tr;
+        s.nbr = b.nbr;
+        s.nnbr = b.nnbr;
+        s.nbr_stride = b.cap;
         s.acc = b.acc;
         s.off = b.g.off;
         s.map = b.map;
@@ -98,7 +101,11 @@ cudaError_t tss_solver::mark(int k, cudaStream_t s) {
 // Enqueue one step (the body of AdvanceTS, WCSPHSolver.cu:2726-2810).
 cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
     cudaError_t e;
-    const StepView V = view();
+    StepView V = view();
+    // the force passes read the neighbour lists their scale's density pass records
+    // when that pass runs one particle per thread
+    if (launch.per_warp[1]) V.L.nbr = nullptr;
+    if (launch.per_warp[0]) V.H.nbr = nullptr;
     if ((e = mark(0, s)) != cudaSuccess) return e;
     // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid);
     //    their key pass ran at the end of the previous step (force kernels, split),
@@ -474,6 +481,9 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
         A.add(&b.pres, cap);
         A.add(&b.q, cap);
         A.add(&b.tr, cap);
+        A.add(&b.nbr, static_cast<size_t>(kMaxNbr) * (cap > 0 ? cap : 1));
+        A.add(&b.nnbr, cap);
+        b.cap = cap > 0 ? cap : 1;
         A.add(&b.ndens, s->carry ? cap : 1);
         A.add(&b.npres, s->carry ? cap : 1);
     };

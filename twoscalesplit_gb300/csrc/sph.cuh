@@ -17,6 +17,15 @@ struct ScaleView {
     float* pres;
     float* q;        // p / rho^2
     float* tr;       // low scale: each split parent's tether radius, written by the low-res force
+    // Neighbour lists the density pass records for the force pass of the same scale
+    // (one particle per thread): entry c of sorted particle i is
+    // nbr[c * nbr_stride + i] = j - i for its c-th same-scale neighbour within the
+    // density's support (itself left out), in window order; nnbr[i] is their count,
+    // kNbrOverflow when there are more than kMaxNbr or an offset does not fit 16
+    // bits.  Null when the density pass of this step did not record them.
+    int16_t* nbr;
+    uint8_t* nnbr;
+    int nbr_stride;
     float2* acc;
     const int* off;  // dense cell offsets [C+1]
     int32_t* map;    // slot id -> index in the cur arrays
@@ -49,6 +58,9 @@ struct StepView {
     const uint16_t* scL;
     const uint16_t* scH;
 };
+
+constexpr int kMaxNbr = 20;
+constexpr uint8_t kNbrOverflow = 255;
 
 constexpr int kSplitThreads = 256;
 constexpr int kSplitItems = 16;

@@ -53,6 +53,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s"
 GATHER_STAGES = ("density_high", "density_low", "force_low", "force_high")
+NBR_BYTES = 25
 UNIT = "particle-steps/s"
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
@@ -71,16 +72,18 @@ def stage_bytes(stage, n_low, n_high, c_low, c_high, carry, n_fresh_children, re
         return grid(n_low, c_low)
     if stage == "relax":  # per sub-step, per child: R pos, vel (16); W dens, pres (8); W pos, vel twice (32)
         return n_fresh_children * relax_iters * 56
+    # the density passes also write each particle's neighbour list (~12 16-bit
+    # offsets and a count: 25 B), which the force passes read back
     if stage == "density_high":
-        return n_high * 21 + 4 * c_high
+        return n_high * (21 + NBR_BYTES) + 4 * c_high
     if stage == "density_low":
-        return n_low * 21 + 4 * c_low
+        return n_low * (21 + NBR_BYTES) + 4 * c_low
     if stage == "force_low":
-        return n_low * (59 + (12 if carry else 0)) + 4 * c_low
+        return n_low * (59 + NBR_BYTES + (12 if carry else 0)) + 4 * c_low
     if stage == "split":
         return n_low * 1
     if stage == "force_high":
-        return n_high * (78 + (12 if carry else 0)) + 4 * c_low
+        return n_high * (78 + NBR_BYTES + (12 if carry else 0)) + 4 * c_low
     return 0
 
 

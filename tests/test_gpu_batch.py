@@ -31,11 +31,15 @@ def _mixed_scenes(relax):
     return out
 
 
-@pytest.mark.parametrize("relax", [0, 4])
-def test_batch_scenes_equal_alone(relax):
+@pytest.mark.parametrize("relax,arith", [(0, "exact"), (4, "exact"), (0, "fast"), (4, "fast")])
+def test_batch_scenes_equal_alone(relax, arith):
+    """in either arithmetic: the tolerance arithmetic's pair terms are rounded the
+    same way in the batched and the single-scene kernel forms"""
     scs = _mixed_scenes(relax)
     batch = Batch(scs)
     alone = [Solver.from_scene(sc) for sc in scs]
+    for s in [batch] + alone:
+        s.set_arith(arith)
     steps = 90
     batch.step(steps)
     for a in alone:

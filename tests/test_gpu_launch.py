@@ -60,6 +60,21 @@ def test_every_shape_gives_the_same_steps(threads, persistent, per_warp):
     _assert_same(_state(ref), _state(sol))
 
 
+@pytest.mark.parametrize("threads,persistent,per_warp", [(64, True, True), (128, False, False), (256, True, True)])
+def test_every_shape_gives_the_same_steps_in_the_tolerance_arithmetic(threads, persistent, per_warp):
+    sc = _scene()
+    ref = Solver.from_scene(sc)
+    ref.set_arith("fast")
+    ref.step(60)
+    sol = Solver.from_scene(sc)
+    sol.set_arith("fast")
+    sol.set_launch(_shape(threads, persistent, per_warp))
+    sol.step(60)
+    sol.sync()
+    assert sol.counts()["n_high"] > 0
+    _assert_same(_state(ref), _state(sol))
+
+
 def test_shape_of_a_batch_does_not_change_its_scenes():
     scs = [_scene(seed=s, relax=0) for s in (5, 6, 7)]
     a, b = Batch(scs), Batch(scs)

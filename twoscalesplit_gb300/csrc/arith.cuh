@@ -74,6 +74,13 @@ struct ExactArith {
     }
 };
 
+// Every value FastArith hands to a sum (the pair's terms, a kernel's two halves)
+// comes from the scalar __fmul_rn / __fadd_rn intrinsics, which are never merged
+// into a fused multiply-add, so the bits do not depend on how the compiler
+// schedules one kernel form or another: the batched and single-scene forms, and
+// the one-particle-per-thread and per-warp walks, give the same results, as in the
+// exact arithmetic.  (A packed product feeding an add can be fused by the compiler
+// even with --fmad=false, and it was, differently in different kernel forms.)
 struct FastArith {
     static constexpr bool kFast = true;
 
@@ -96,26 +103,27 @@ struct FastArith {
                                       q.y < 1.0f ? w1.y : (q.y < 2.0f ? w2.y : 0.0f));
         const float2 gs = make_float2(q.x < 1.0f ? g1.x : (q.x < 2.0f ? g2.x : 0.0f),
                                       q.y < 1.0f ? g1.y : (q.y < 2.0f ? g2.y : 0.0f));
-        const float2 wc = __fmul2_rn(ws, P.fC);
-        const float2 gc = __fmul2_rn(gs, P.fG);
-        w = wc.x + wc.y;
-        c = gc.x + gc.y;
+        w = __fadd_rn(__fmul_rn(ws.x, P.fC.x), __fmul_rn(ws.y, P.fC.y));
+        c = __fadd_rn(__fmul_rn(gs.x, P.fG.x), __fmul_rn(gs.y, P.fG.y));
     }
 
     template <int HS>
     __device__ __forceinline__ static PairTerms pair(const Params& P, float2 pij, float x, float2 vij, float qi,
                                                      float qj, float densi, float densj) {
         const float rinv = rsqrt_approx(x);
-        const float d = x * rinv;
+        const float d = __fmul_rn(x, rinv);
         float w, c;
         kernels(P, x, rinv, d, w, c);
-        const float dvp = __fmaf_rn(vij.x, pij.x, vij.y * pij.y);
+        const float dvp = __fmaf_rn(vij.x, pij.x, __fmul_rn(vij.y, pij.y));
         const float eps = HS == kHLow ? P.fEps.x : (HS == kHCross ? P.fEps.y : P.fEps.z);
         const float kv = HS == kHLow ? P.fKv.x : (HS == kHCross ? P.fKv.y : P.fKv.z);
-        const float visc = dvp * kv * rcp_approx((x + eps) * (densi + densj));
-        const float coeff = dvp < 0.0f ? (qi + qj) - visc : qi + qj;
-        const float s = coeff * c;
-        return PairTerms{__fmul2_rn(make_float2(s, s), pij), __fmul2_rn(make_float2(w, w), pij)};
+        const float den = __fmul_rn(__fadd_rn(x, eps), __fadd_rn(densi, densj));
+        const float visc = __fmul_rn(__fmul_rn(dvp, kv), rcp_approx(den));
+        const float qs = __fadd_rn(qi, qj);
+        const float coeff = dvp < 0.0f ? __fsub_rn(qs, visc) : qs;
+        const float s = __fmul_rn(coeff, c);
+        return PairTerms{make_float2(__fmul_rn(s, pij.x), __fmul_rn(s, pij.y)),
+                         make_float2(__fmul_rn(w, pij.x), __fmul_rn(w, pij.y))};
     }
 
     // (W_r(d) + W_rh(d)) / 2 at d = sqrt(x)
@@ -129,21 +137,20 @@ struct FastArith {
         const float2 w2 = __fmul2_rn(__fmul2_rn(a, a), a);
         const float2 ws = make_float2(q.x < 1.0f ? w1.x : (q.x < 2.0f ? w2.x : 0.0f),
                                       q.y < 1.0f ? w1.y : (q.y < 2.0f ? w2.y : 0.0f));
-        const float2 wc = __fmul2_rn(ws, P.fC);
-        return wc.x + wc.y;
+        return __fadd_rn(__fmul_rn(ws.x, P.fC.x), __fmul_rn(ws.y, P.fC.y));
     }
 
     // Gamma_rad(d) = 0.02 c^2 / d^2 * {2/3; 2q - 1.5q^2 = q (2 - 1.5q); 0.5 (2-q)^2; 0}
     template <int S>
     __device__ __forceinline__ static float2 wall(const Params& P, float2 pik, float x, float cB) {
         const float d = sqrt_approx(x);
-        const float q = d * (S ? P.fTor.y : P.fTor.x);
-        const float a = 2.0f - q;
-        const float r2 = q * __fmaf_rn(-1.5f, q, 2.0f);
-        const float r3 = 0.5f * a * a;
+        const float q = __fmul_rn(d, S ? P.fTor.y : P.fTor.x);
+        const float a = __fsub_rn(2.0f, q);
+        const float r2 = __fmul_rn(q, __fmaf_rn(-1.5f, q, 2.0f));
+        const float r3 = __fmul_rn(__fmul_rn(0.5f, a), a);
         const float f = q < 2.0f / 3.0f ? 2.0f / 3.0f : (q < 1.0f ? r2 : (q < 2.0f ? r3 : 0.0f));
-        const float gm = cB * P.fKw * rcp_approx(x) * f;
-        return make_float2(gm * pik.x, gm * pik.y);
+        const float gm = __fmul_rn(__fmul_rn(__fmul_rn(cB, P.fKw), rcp_approx(x)), f);
+        return make_float2(__fmul_rn(gm, pik.x), __fmul_rn(gm, pik.y));
     }
 };
 

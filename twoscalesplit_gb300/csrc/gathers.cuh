@@ -59,20 +59,28 @@ using namespace gather_detail;
 // the ~36 candidates of the window, of which about a third are accepted.  A
 // particle with more than kMaxNbr neighbours, or one whose offset does not fit
 // 16 bits, is marked and walks its window.
+//
+// The entries are staged in shared memory as they are found (`col`: the thread's
+// column of a kMaxNbr x kNbrCols array, stride kNbrCols) and written out after the
+// walk, entry c of every lane together, so that a warp's stores to the transposed
+// global array coalesce; stored as found, they scattered over its rows.
+constexpr int kNbrCols = 256;  // the gathers' largest block
+
 struct NbrRecord {
-    int16_t* nbr;
-    int stride, i, n;
+    int16_t* col;
+    int i, n;
     bool ok;
-    __device__ __forceinline__ NbrRecord(const ScaleView& S, int i_)
-        : nbr(S.nbr), stride(S.nbr_stride), i(i_), n(0), ok(true) {}
+    __device__ __forceinline__ NbrRecord(int i_, int16_t* col_) : col(col_), i(i_), n(0), ok(true) {}
     __device__ __forceinline__ void add(int j) {
         if (j == i) return;  // the density's self term: never a force pair
         const int dj = j - i;
-        if (n < kMaxNbr && dj >= -32768 && dj <= 32767) nbr[n * stride + i] = static_cast<int16_t>(dj);
+        if (n < kMaxNbr && dj >= -32768 && dj <= 32767) col[n * kNbrCols] = static_cast<int16_t>(dj);
         else ok = false;
         ++n;
     }
     __device__ __forceinline__ void finish(const ScaleView& S) const {
+        if (ok)
+            for (int c = 0; c < n; ++c) S.nbr[c * S.nbr_stride + i] = col[c * kNbrCols];
         S.nnbr[i] = ok ? static_cast<uint8_t>(n) : kNbrOverflow;
     }
 };
@@ -98,7 +106,8 @@ __device__ __forceinline__ void list_or_walk(const ScaleView& S, int i, Test&& t
 // High-res density + Tait, computeParticleDensityPressureHigh (WCSPHSolver.cu:1426-1516)
 // ---------------------------------------------------------------------------
 template <class A, class G>
-__device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i, bool hstate0) {
+__device__ __forceinline__ void density_high_one(const Params& P, const StepView& V, int i, bool hstate0,
+                                                 int16_t* nbr_col) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     const int* offH = H.off + P.cbH;
@@ -109,7 +118,7 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
     float x = 0.0f;
     const auto term = [&](int) { return A::density(P, x); };
     const bool rec_on = !G::kWarp && H.nbr != nullptr;
-    NbrRecord rec(H, i);
+    NbrRecord rec(i, nbr_col);
     int csx, csy, cex, cey;
     grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
     grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
@@ -199,13 +208,15 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
 
 template <bool B, class G, class A>
 __global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
+    __shared__ int16_t s_nbr[G::kWarp ? 1 : kMaxNbr * kNbrCols];
+    int16_t* const nbr_col = s_nbr + (G::kWarp ? 0 : threadIdx.x);
     const bool hstate0 = V.cnt->h_state0 != 0;
     for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];
-            density_high_one<A, G>(P, V, i, hstate0);
+            density_high_one<A, G>(P, V, i, hstate0, nbr_col);
         } else {
-            density_high_one<A, G>(P0, V, i, hstate0);
+            density_high_one<A, G>(P0, V, i, hstate0, nbr_col);
         }
     });
 }
@@ -214,7 +225,8 @@ __global__ void __launch_bounds__(256) k_density_high(Params P0, StepView V) {
 // Low-res density + Tait, computeParticleDensityPressure (WCSPHSolver.cu:1342-1424)
 // ---------------------------------------------------------------------------
 template <class A, class G>
-__device__ __forceinline__ void density_low_one(const Params& P, const StepView& V, int i, bool cross) {
+__device__ __forceinline__ void density_low_one(const Params& P, const StepView& V, int i, bool cross,
+                                                int16_t* nbr_col) {
     const ScaleView& H = V.H;
     const ScaleView& L = V.L;
     const float2 p = L.pos[i];
@@ -223,7 +235,7 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
     float x = 0.0f;
     const auto term = [&](int) { return A::density(P, x); };
     const bool rec_on = !G::kWarp && L.nbr != nullptr;
-    NbrRecord rec(L, i);
+    NbrRecord rec(i, nbr_col);
     int csx, csy, cex, cey;
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
@@ -265,13 +277,15 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
 
 template <bool B, class G, class A>
 __global__ void __launch_bounds__(256) k_density_low(Params P0, StepView V) {
+    __shared__ int16_t s_nbr[G::kWarp ? 1 : kMaxNbr * kNbrCols];
+    int16_t* const nbr_col = s_nbr + (G::kWarp ? 0 : threadIdx.x);
     const bool cross = V.cnt->h_state0 != 0;
     for_each_particle<G>(V.cnt->cur[0], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scL[i]];
-            density_low_one<A, G>(P, V, i, cross);
+            density_low_one<A, G>(P, V, i, cross, nbr_col);
         } else {
-            density_low_one<A, G>(P0, V, i, cross);
+            density_low_one<A, G>(P0, V, i, cross, nbr_col);
         }
     });
 }

@@ -413,6 +413,11 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
         // (rounding is monotone), so the children's clamp is unchanged bit for bit.
         if (s == 1u)
             L.tr[i] = static_cast<float>(0.75 * sqrt(static_cast<double>(P.mL) / (static_cast<double>(dens) * kPi)));
+        // the cells of this step's grid that hold an entry in state 0 after the split
+        // marks: the only low-res partners of a state-1 child in the high-res force.
+        // The entry's cell is the one its key was made from (its position at the
+        // start of the step, the same cell function).
+        if (ns == 0u) L.cflag[P.cbL + cell_hash_s<0>(P, L.pos[i])] = static_cast<uint8_t>(V.cnt->steps);
         L.npos[i] = p;
         L.nvel[i] = v;
         L.nid[i] = L.id[i];
@@ -500,8 +505,20 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
     PairTerms fl{make_float2(0.f, 0.f), fh.t};  // (accL, accT): the sigma sum continues
-    G::window(
+    // A state-1 child pairs only with low-res entries in state 0 (lambda_HL and
+    // notDeleted); a row of the window whose cells the low-res force did not stamp
+    // in this step holds none, and is skipped.
+    const bool odd = (s & 1u) != 0u;
+    const uint8_t stamp = static_cast<uint8_t>(V.cnt->steps);
+    G::window_if(
         L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
+        [&](int row) {
+            if (!odd) return true;
+            const uint8_t* f = L.cflag + P.cbL + row;
+            for (int cx = csx; cx <= cex; ++cx)
+                if (f[cx] == stamp) return true;
+            return false;
+        },
         [&](int k) {
             const unsigned sj = L.nst[k];  // low-res states after this step's split marks
             if (!(lamHL(s, sj) && notDeleted(sj))) return false;

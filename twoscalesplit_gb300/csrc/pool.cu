@@ -222,6 +222,8 @@ void plan_pool(tss_solver* s, const tss_pool_config& c, Arena& A, PoolPlan& pp) 
     };
     scale(s->L, Ls, s->slotsL);
     scale(s->H, Hc > 0 ? Hc : 1, s->slotsH);
+    A.add(&s->L.cflag, CLc);
+    A.add(&s->H.cflag, 1);
     A.add(&pp.gL, grid_bufs_bytes(Ls, CLc));
     A.add(&pp.gH, grid_bufs_bytes(Hc > 0 ? Hc : 1, CHc));
     A.add(&pp.gW, grid_bufs_bytes(Wc > 0 ? Wc : 1, CLc));

@@ -26,6 +26,7 @@ StepView tss_solver::view() const {
         s.pres = b.pres;
         s.q = b.q;
         s.tr = b.tr;
+        s.cflag = b.cflag;
         s.nbr = b.nbr;
         s.nnbr = b.nnbr;
         s.nbr_stride = b.cap;
@@ -489,6 +490,8 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
     };
     scale(s->L, n_low, s->slotsL);
     scale(s->H, cap_high, s->slotsH);
+    A.add(&s->L.cflag, s->CL);
+    A.add(&s->H.cflag, 1);
     char* gL = nullptr;
     char* gH = nullptr;
     char* gW = nullptr;

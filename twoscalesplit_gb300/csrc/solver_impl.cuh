@@ -32,6 +32,7 @@ struct ScaleBufs {
     int32_t *id, *nid, *map;
     float *dens, *pres, *q, *ndens, *npres;
     float* tr;  // low scale: a split parent's tether radius this step (sorted order)
+    uint8_t* cflag;  // low scale: per cell, the step stamp of a cell with an unsplit entry (see ScaleView)
     int16_t* nbr;  // neighbour lists, kMaxNbr x cap (see ScaleView)
     uint8_t* nnbr;
     int cap;       // entries of the sorted arrays

@@ -17,6 +17,10 @@ struct ScaleView {
     float* pres;
     float* q;        // p / rho^2
     float* tr;       // low scale: each split parent's tether radius, written by the low-res force
+    // low scale, one byte per cell: the low-res force sets a cell to the step counter
+    // (mod 256) when the cell holds an entry in state 0 after the split marks.  Any
+    // other value only makes the high-res force walk a row it could skip.
+    uint8_t* cflag;
     // Neighbour lists the density pass records for the force pass of the same scale
     // (one particle per thread): entry c of sorted particle i is
     // nbr[c * nbr_stride + i] = j - i for its c-th same-scale neighbour within the

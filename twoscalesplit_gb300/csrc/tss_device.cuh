@@ -317,48 +317,9 @@ __device__ __forceinline__ float pair_density(const Params& P, float d) {
     return (w.x + w.y) / 2.0f;
 }
 
-// Candidates of a cell window, row by row (cells in x order, particles in cell
-// order: the reference's summation order).  next() returns the next candidate that
-// `accept` takes, or -1.  Each lane skips rejected candidates on its own and the
-// search loop has a single exit, so the lanes meet again before the caller's pair
-// arithmetic, which then runs with the warp converged instead of at the in-range
-// fraction of the lanes.
-struct Window {
-    const int* off;
-    int dimx, csx, cex, cy, cey, j, b;
-    __device__ __forceinline__ Window() : off(nullptr), dimx(0), csx(0), cex(0), cy(1), cey(0), j(0), b(0) {}
-    __device__ __forceinline__ Window(const int* off_, int dimx_, int csx_, int cex_, int csy_, int cey_)
-        : off(off_), dimx(dimx_), csx(csx_), cex(cex_), cy(csy_), cey(cey_) {
-        const int row = cy * dimx;
-        j = off[row + csx];
-        b = off[row + cex + 1];
-    }
-    template <class Accept>
-    __device__ __forceinline__ int next(Accept&& accept) {
-        int found = -1;
-        while (true) {
-            if (j >= b) {
-                if (++cy > cey) break;
-                const int row = cy * dimx;
-                j = off[row + csx];
-                b = off[row + cex + 1];
-                continue;
-            }
-            const int k = j++;
-            if (accept(k)) {
-                found = k;
-                break;
-            }
-        }
-        return found;
-    }
-};
-
 __device__ __forceinline__ float sq(float2 v) {
     const float2 m = mul2(v, v);
     return m.x + m.y;
 }
-
-
 
 }  // namespace tss

@@ -90,6 +90,34 @@ def test_pool_admit_retire_extract_equal_alone(relax):
     assert sum(x[1]["id"].shape[0] for x in (got_a, got_b, got_c)) > 0  # splits happened
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_pool_whose_neighbour_list_columns_pass_2_31_entries(arith):
+    """A pool sized for 300M high-res particles: entry c of a particle's neighbour
+    list lies c x 300M entries into the list array, past 2^31 from c = 8 on, so a
+    32-bit index would wrap into other arrays.  The scene must still give its state
+    alone, bit for bit, in either arithmetic (about 33 GB of device memory)."""
+    rng = np.random.default_rng(5)
+    sc = scenes.mixed_scene(rng, n_min=4000, n_max=6000)
+    f = footprint(sc)
+    cfg = pool_config(low_slots=f["low_slots"], high_particles=300_000_000, low_cells=f["low_cells"],
+                      high_cells=f["high_cells"], wall_particles=f["wall_particles"], max_scenes=2)
+    assert 8 * cfg.high_particles > 2**31
+    pool = Pool(cfg)
+    pool.set_arith(arith)
+    sid = pool.admit(sc)
+    pool.step(40)
+    got = pool.extract(sid)
+    pool.sync()
+    assert pool.counts()["error_bits"] == 0
+    sol = Solver.from_scene(sc)
+    sol.set_arith(arith)
+    sol.step(40)
+    sol.sync()
+    _assert_same([sol.download(TSS_SCALE_LOW), sol.download(TSS_SCALE_HIGH)], got, arith)
+    assert got[1]["id"].shape[0] > 0  # splits happened: the high-res lists were in use
+    pool.close()
+
+
 def test_pool_download_scene_matches_extract_and_frees_pages():
     scs = _scenes(0, n=3, seed=5)
     fp = [footprint(s) for s in scs]

@@ -79,8 +79,8 @@ struct ExactArith {
 // into a fused multiply-add, so the bits do not depend on how the compiler
 // schedules one kernel form or another: the batched and single-scene forms, and
 // the one-particle-per-thread and per-warp walks, give the same results, as in the
-// exact arithmetic.  (A packed product feeding an add can be fused by the compiler
-// even with --fmad=false, and it was, differently in different kernel forms.)
+// exact arithmetic.  (--fmad=false does not keep a packed product apart from the
+// packed add it feeds: that was measured in the exact arithmetic's kernel pairs.)
 struct FastArith {
     static constexpr bool kFast = true;
 

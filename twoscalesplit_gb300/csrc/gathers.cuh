@@ -79,8 +79,10 @@ struct NbrRecord {
         ++n;
     }
     __device__ __forceinline__ void finish(const ScaleView& S) const {
-        if (ok)
-            for (int c = 0; c < n; ++c) S.nbr[c * S.nbr_stride + i] = col[c * kNbrCols];
+        if (ok) {
+            int16_t* dst = S.nbr + i;  // 64-bit steps: a pool's capacity times kMaxNbr passes 2^31
+            for (int c = 0; c < n; ++c, dst += S.nbr_stride) *dst = col[c * kNbrCols];
+        }
         S.nnbr[i] = ok ? static_cast<uint8_t>(n) : kNbrOverflow;
     }
 };
@@ -92,8 +94,9 @@ __device__ __forceinline__ void list_or_walk(const ScaleView& S, int i, Test&& t
     if constexpr (!G::kWarp) {
         const int nc = S.nbr ? S.nnbr[i] : kNbrOverflow;
         if (nc != kNbrOverflow) {
-            for (int c = 0; c < nc; ++c) {
-                const int k = i + S.nbr[c * S.nbr_stride + i];
+            const int16_t* src = S.nbr + i;
+            for (int c = 0; c < nc; ++c, src += S.nbr_stride) {
+                const int k = i + *src;
                 if (test(k)) add(sum, term(k));
             }
             return;
@@ -298,6 +301,12 @@ template <class A, class G, int S>
 __device__ __forceinline__ float2 wall_sum(const Params& P, const StepView& V, float2 p, int csx, int cex, int csy,
                                            int cey, float Tle, float cB) {
     float2 accB = make_float2(0.f, 0.f);
+    // A window of at most four cells a side from (csx, csy) lies within two cells of
+    // (mx, my); with no wall particle there the sum is empty.
+    if (cex - csx <= 3 && cey - csy <= 3) {
+        const int mx = min(csx + 1, P.dimL[0] - 1), my = min(csy + 1, P.dimL[1] - 1);
+        if (!V.wnear[P.cbL + my * P.dimL[0] + mx]) return accB;
+    }
     const int* woff = V.woff + P.cbL;
     const float2* wpos = V.wpos + P.wb;
     float2 pik = make_float2(0.f, 0.f);

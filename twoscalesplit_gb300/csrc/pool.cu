@@ -224,6 +224,7 @@ void plan_pool(tss_solver* s, const tss_pool_config& c, Arena& A, PoolPlan& pp) 
     scale(s->H, Hc > 0 ? Hc : 1, s->slotsH);
     A.add(&s->L.cflag, CLc);
     A.add(&s->H.cflag, 1);
+    A.add(&s->wnear, CLc);
     A.add(&pp.gL, grid_bufs_bytes(Ls, CLc));
     A.add(&pp.gH, grid_bufs_bytes(Hc > 0 ? Hc : 1, CHc));
     A.add(&pp.gW, grid_bufs_bytes(Wc > 0 ? Wc : 1, CLc));
@@ -441,6 +442,7 @@ tss_status admit(tss_solver* s, const SceneIn& in, cudaStream_t st, int* scene_i
     } else if (e == cudaSuccess) {
         e = cudaMemsetAsync(s->woff + cbL, 0, sizeof(int) * (static_cast<size_t>(CLs) + 1), st);
     }
+    if (e == cudaSuccess) launch_wall_near(s->woff + cbL, s->wnear + cbL, P.dimL[0], P.dimL[1], st);
     if (e == cudaSuccess) {
         k_set_int<<<1, 1, 0, st>>>(s->usedL, static_cast<int>(s->ex_cellsL.high_water()));
         k_set_int<<<1, 1, 0, st>>>(s->usedH, static_cast<int>(s->ex_cellsH.high_water()));

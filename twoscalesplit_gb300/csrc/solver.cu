@@ -53,6 +53,7 @@ StepView tss_solver::view() const {
     }
     v.wpos = wpos;
     v.woff = woff;
+    v.wnear = wnear;
     v.cnt = cnt;
     v.split_flag = split_flag;
     v.split_ids = split_ids;
@@ -492,6 +493,7 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
     scale(s->H, cap_high, s->slotsH);
     A.add(&s->L.cflag, s->CL);
     A.add(&s->H.cflag, 1);
+    A.add(&s->wnear, s->CL);
     char* gL = nullptr;
     char* gH = nullptr;
     char* gW = nullptr;
@@ -563,6 +565,7 @@ tss_status create_solver(const SceneIn& sc, int cap_high, tss_solver** out) {
         if (e == cudaSuccess)
             e = grid_build_enqueue(wraw, wid, nW_dev, n_wall, s->P.ox, s->P.oy, s->P.r, s->P.dimL[0], s->P.dimL[1],
                                    gw, a, &s->cnt->err, st);
+        if (e == cudaSuccess) launch_wall_near(s->woff, s->wnear, s->P.dimL[0], s->P.dimL[1], st);
     }
     if (e == cudaSuccess) e = s->prime_keys(st);
     if (e == cudaSuccess) e = cudaGetLastError();

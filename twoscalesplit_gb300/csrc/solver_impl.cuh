@@ -108,6 +108,7 @@ struct tss_solver {
     tss::ScaleBufs L{}, H{};
     float2* wpos = nullptr;
     int* woff = nullptr;
+    uint8_t* wnear = nullptr;  // per low cell (StepView::wnear)
     tss::Counters* cnt = nullptr;
     uint8_t* split_flag = nullptr;
     int32_t* split_ids = nullptr;

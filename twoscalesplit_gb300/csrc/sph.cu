@@ -315,6 +315,31 @@ int gather_occupancy(int g, bool batched, bool warp, bool fast, int threads) {
                 : gather_occupancy_a<ExactArith>(g, batched, warp, threads);
 }
 
+// Walls do not move: once per scene, each low cell records whether a wall particle
+// lies in a cell within two cells of it (Chebyshev distance, inside the grid).
+__global__ void k_wall_near(const int* __restrict__ woff, uint8_t* __restrict__ wnear, int dimx, int dimy) {
+    const long long n = static_cast<long long>(dimx) * dimy;
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int cx = static_cast<int>(c % dimx), cy = static_cast<int>(c / dimx);
+        const int x0 = max(cx - 2, 0), x1 = min(cx + 2, dimx - 1);
+        bool any = false;
+        for (int y = max(cy - 2, 0); y <= min(cy + 2, dimy - 1); ++y) {
+            const long long row = static_cast<long long>(y) * dimx;
+            any |= woff[row + x0] != woff[row + x1 + 1];
+        }
+        wnear[c] = any ? 1 : 0;
+    }
+}
+
+void launch_wall_near(const int* woff, uint8_t* wnear, int dimx, int dimy, cudaStream_t s) {
+    const long long n = static_cast<long long>(dimx) * dimy;
+    if (n <= 0) return;
+    const long long want = (n + 255) / 256;
+    const int blocks = static_cast<int>(want < 16LL * sm_count() ? want : 16LL * sm_count());
+    k_wall_near<<<blocks, 256, 0, s>>>(woff, wnear, dimx, dimy);
+}
+
 #define TSS_LAUNCHER(NAME)                                                                        \
     void launch_##NAME(bool batched, int blocks, int threads, cudaStream_t s, const Params& P,   \
                        const StepView& V) {                                                       \

@@ -29,7 +29,7 @@ struct ScaleView {
     // bits.  Null when the density pass of this step did not record them.
     int16_t* nbr;
     uint8_t* nnbr;
-    int nbr_stride;
+    long long nbr_stride;  // entries per list column: the scale's capacity
     float2* acc;
     const int* off;  // dense cell offsets [C+1]
     int32_t* map;    // slot id -> index in the cur arrays
@@ -50,6 +50,7 @@ struct StepView {
     ScaleView L, H;
     const float2* wpos;     // walls: each scene's in (low cell, id) order from its wall base
     const int* woff;        // wall cell offsets on the low grid
+    const uint8_t* wnear;   // per low cell: 1 when a cell within two cells of it holds a wall particle
     Counters* cnt;
     uint8_t* split_flag;    // [n_low]
     int32_t* split_ids;     // [n_low] parents split this step (= next step's fresh list)
@@ -91,5 +92,8 @@ void launch_k_relax_density(bool batched, int blocks, int threads, cudaStream_t 
 void launch_k_relax_force(bool batched, int blocks, int threads, cudaStream_t s, const Params& P, const StepView& V);
 // resident blocks per SM of gather g at `threads` threads per block; 0 on error
 int gather_occupancy(int g, bool batched, bool warp, bool fast, int threads);
+// wnear of one scene's dimx x dimy low grid from its wall cell offsets (both
+// pointers at the scene's first cell), after its wall grid is built
+void launch_wall_near(const int* woff, uint8_t* wnear, int dimx, int dimy, cudaStream_t s);
 
 }  // namespace tss

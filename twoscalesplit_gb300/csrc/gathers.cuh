@@ -87,17 +87,55 @@ struct NbrRecord {
     }
 };
 
-// The force pass's same-scale pairs: from the list when there is one, else `walk`.
+// A same-scale neighbour's state as the force pass reads it.
+struct NbrState {
+    float2 pos, vel;
+    float q, dens;
+    unsigned st;
+};
+__device__ __forceinline__ NbrState fetch_nbr(const ScaleView& S, int k) {
+    return NbrState{S.pos[k], S.vel[k], S.q[k], S.dens[k], S.st[k]};
+}
+
+// Entries of a neighbour list taken per trip of the force pass's list walk.
+constexpr int kListPairsPerTrip = 2;
+
+// The force pass's same-scale pairs: from the list when there is one (test and
+// term take the neighbour's NbrState), else `walk`.  Two entries per trip: both
+// neighbours' state is loaded before either pair is evaluated, in list order, so
+// that a thread has two neighbours' loads in flight (the force kernels wait mostly
+// on these loads).
 template <class G, class T, class Test, class Term, class Add, class Walk>
 __device__ __forceinline__ void list_or_walk(const ScaleView& S, int i, Test&& test, Term&& term, Add&& add,
                                              T& sum, Walk&& walk) {
     if constexpr (!G::kWarp) {
         const int nc = S.nbr ? S.nnbr[i] : kNbrOverflow;
         if (nc != kNbrOverflow) {
+            const long long stride = S.nbr_stride;
             const int16_t* src = S.nbr + i;
-            for (int c = 0; c < nc; ++c, src += S.nbr_stride) {
-                const int k = i + *src;
-                if (test(k)) add(sum, term(k));
+            int c = 0;
+            if constexpr (kListPairsPerTrip == 4) {
+                for (; c + 3 < nc; c += 4, src += 4 * stride) {
+                    const int k0 = i + src[0], k1 = i + src[stride], k2 = i + src[2 * stride], k3 = i + src[3 * stride];
+                    const NbrState n0 = fetch_nbr(S, k0), n1 = fetch_nbr(S, k1), n2 = fetch_nbr(S, k2),
+                                   n3 = fetch_nbr(S, k3);
+                    if (test(n0)) add(sum, term(n0));
+                    if (test(n1)) add(sum, term(n1));
+                    if (test(n2)) add(sum, term(n2));
+                    if (test(n3)) add(sum, term(n3));
+                }
+            }
+            if constexpr (kListPairsPerTrip >= 2) {
+                for (; c + 1 < nc; c += 2, src += 2 * stride) {
+                    const int k0 = i + src[0], k1 = i + src[stride];
+                    const NbrState n0 = fetch_nbr(S, k0), n1 = fetch_nbr(S, k1);
+                    if (test(n0)) add(sum, term(n0));
+                    if (test(n1)) add(sum, term(n1));
+                }
+            }
+            for (; c < nc; ++c, src += stride) {
+                const NbrState n0 = fetch_nbr(S, i + *src);
+                if (test(n0)) add(sum, term(n0));
             }
             return;
         }
@@ -125,16 +163,14 @@ __device__ __forceinline__ void density_high_one(const Params& P, const StepView
     int csx, csy, cex, cey;
     grid_coord_s<1>(P, p.x, p.y, -P.rh, csx, csy);
     grid_coord_s<1>(P, p.x, p.y, P.rh, cex, cey);
-    G::window(
+    // a candidate the lambda mask rejects gets key +inf: no cutoff passes it
+    G::template window_keyed<4>(
         offH, P.dimH[0], csx, cex, csy, cey,
-        [&](int k) {
-            if (!lamHH(s, H.st[k])) return false;
-            x = sq(sub(p, H.pos[k]));
-            return x <= P.Tle_rh;
-        },
-        [&](int j) {
+        [&](int k) { return lamHH(s, H.st[k]) ? sq(sub(p, H.pos[k])) : INFINITY; },
+        [&](float xk) { return xk <= P.Tle_rh; },
+        [&](int j, float xj) {
             if (rec_on) rec.add(j);
-            return A::density(P, x);
+            return A::density(P, xj);
         },
         add_density, d);
     if (rec_on) rec.finish(H);
@@ -242,15 +278,12 @@ __device__ __forceinline__ void density_low_one(const Params& P, const StepView&
     int csx, csy, cex, cey;
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);
     grid_coord_s<0>(P, p.x, p.y, P.r, cex, cey);
-    G::window(
-        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey,
-        [&](int k) {
-            x = sq(sub(p, L.pos[k]));
-            return x <= P.Tle_r;
-        },
-        [&](int j) {
+    G::template window_keyed<2>(
+        L.off + P.cbL, P.dimL[0], csx, cex, csy, cey, [&](int k) { return sq(sub(p, L.pos[k])); },
+        [&](float xk) { return xk <= P.Tle_r; },
+        [&](int j, float xj) {
             if (rec_on) rec.add(j);
-            return A::density(P, x);
+            return A::density(P, xj);
         },
         add_density, d);
     if (rec_on) rec.finish(L);
@@ -359,7 +392,15 @@ __device__ __forceinline__ bool force_low_one(const Params& P, const StepView& V
         const auto term = [&](int j) {
             return A::template pair<kHLow>(P, pij, x, sub(v, L.vel[j]), qi, L.q[j], dens, L.dens[j]);
         };
-        list_or_walk<G>(L, i, test, term, add_terms, fl,
+        const auto test_n = [&](const NbrState& n) {
+            pij = sub(p, n.pos);
+            x = sq(pij);
+            return x != 0.0f && x <= P.Tlt_r && notDeleted(n.st);
+        };
+        const auto term_n = [&](const NbrState& n) {
+            return A::template pair<kHLow>(P, pij, x, sub(v, n.vel), qi, n.q, dens, n.dens);
+        };
+        list_or_walk<G>(L, i, test_n, term_n, add_terms, fl,
                         [&] { G::window(L.off + P.cbL, P.dimL[0], csx, cex, csy, cey, test, term, add_terms, fl); });
     }
     const float2 accB = wall_sum<A, G, 0>(P, V, p, csx, cex, csy, cey, P.Tle_r, P.cBL);
@@ -508,7 +549,16 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
         const auto term = [&](int j) {
             return A::template pair<kHHigh>(P, pij, x, sub(v, H.vel[j]), qi, H.q[j], dens, H.dens[j]);
         };
-        list_or_walk<G>(H, i, test, term, add_terms, fh,
+        const auto test_n = [&](const NbrState& n) {
+            if (!lamHH(s, n.st)) return false;
+            pij = sub(p, n.pos);
+            x = sq(pij);
+            return x != 0.0f && x <= P.Tlt_rh;
+        };
+        const auto term_n = [&](const NbrState& n) {
+            return A::template pair<kHHigh>(P, pij, x, sub(v, n.vel), qi, n.q, dens, n.dens);
+        };
+        list_or_walk<G>(H, i, test_n, term_n, add_terms, fh,
                         [&] { G::window(H.off + P.cbH, P.dimH[0], csx, cex, csy, cey, test, term, add_terms, fh); });
     }
     grid_coord_s<0>(P, p.x, p.y, -P.r, csx, csy);

@@ -97,14 +97,17 @@ __device__ __forceinline__ NbrState fetch_nbr(const ScaleView& S, int k) {
     return NbrState{S.pos[k], S.vel[k], S.q[k], S.dens[k], S.st[k]};
 }
 
-// Entries of a neighbour list taken per trip of the force pass's list walk.
+// Entries of a neighbour list taken per trip of the force pass's list walk (1 or 2).
 constexpr int kListPairsPerTrip = 2;
 
 // The force pass's same-scale pairs: from the list when there is one (test and
 // term take the neighbour's NbrState), else `walk`.  Two entries per trip: both
 // neighbours' state is loaded before either pair is evaluated, in list order, so
 // that a thread has two neighbours' loads in flight (the force kernels wait mostly
-// on these loads).
+// on these loads).  On a developed 1M-particle dam break that took k_force_high
+// from 0.149 to 0.133 ms (exact) and 0.110 to 0.094 ms (tolerance arithmetic)
+// against one per trip; four per trip was 3-8 % slower than two, with or without
+// one block per SM fewer for the registers.
 template <class G, class T, class Test, class Term, class Add, class Walk>
 __device__ __forceinline__ void list_or_walk(const ScaleView& S, int i, Test&& test, Term&& term, Add&& add,
                                              T& sum, Walk&& walk) {
@@ -114,18 +117,7 @@ __device__ __forceinline__ void list_or_walk(const ScaleView& S, int i, Test&& t
             const long long stride = S.nbr_stride;
             const int16_t* src = S.nbr + i;
             int c = 0;
-            if constexpr (kListPairsPerTrip == 4) {
-                for (; c + 3 < nc; c += 4, src += 4 * stride) {
-                    const int k0 = i + src[0], k1 = i + src[stride], k2 = i + src[2 * stride], k3 = i + src[3 * stride];
-                    const NbrState n0 = fetch_nbr(S, k0), n1 = fetch_nbr(S, k1), n2 = fetch_nbr(S, k2),
-                                   n3 = fetch_nbr(S, k3);
-                    if (test(n0)) add(sum, term(n0));
-                    if (test(n1)) add(sum, term(n1));
-                    if (test(n2)) add(sum, term(n2));
-                    if (test(n3)) add(sum, term(n3));
-                }
-            }
-            if constexpr (kListPairsPerTrip >= 2) {
+            if constexpr (kListPairsPerTrip == 2) {
                 for (; c + 1 < nc; c += 2, src += 2 * stride) {
                     const int k0 = i + src[0], k1 = i + src[stride];
                     const NbrState n0 = fetch_nbr(S, k0), n1 = fetch_nbr(S, k1);

@@ -440,12 +440,13 @@ tss_status tss_solver_get_launch(tss_solver* s, tss_launch* out);
 tss_status tss_solver_set_launch(tss_solver* s, const tss_launch* in);
 /* Launch-shape autotuner: times every candidate shape (threads 64/128/256, covering
  * or persistent grids, one particle per thread; and one particle per warp) on this
- * handle's own steps, keeps the fastest shape of each
- * gather and installs it.  The trial steps are real steps of the handle's state
- * (the shape does not change results); *steps_taken (may be NULL) receives how many
- * were taken: 7 x (steps_per_trial + 1) (six per-thread shapes and one per-warp).  A
- * gather keeps the default shape unless a candidate is more than 5% faster on the
- * trial steps.  Synchronises. */
+ * handle's own steps, stage by stage, and keeps the fastest shape of each gather (a
+ * gather keeps the default shape unless a candidate is more than 5% faster).  Then
+ * it times whole unprofiled steps with that choice, with the default shape and with
+ * one particle per warp throughout, and installs the fastest of the three (the
+ * choice unless another is more than 5% faster).  The trial steps are real steps of
+ * the handle's state (the shape does not change results); *steps_taken (may be
+ * NULL) receives how many were taken: 10 x (steps_per_trial + 1).  Synchronises. */
 tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* best, int* steps_taken);
 
 /* Arithmetic of the gathers' pair terms.  TSS_ARITH_EXACT (the default) is the

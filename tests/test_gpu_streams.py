@@ -68,3 +68,39 @@ def test_steps_on_different_streams_run_in_order():
         assert a["id"].shape[0] > 0
         for k in ("id", "pos", "vel", "state"):
             assert np.array_equal(a[k], b[k]), (scale, k)
+
+
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_branched_step_graph_equals_sequential(arith):
+    """Outside profiling a step graph runs the two grid builds and the two density
+    passes as parallel branches; with profiling on it runs every stage in order.
+    Both must give the same state, bit for bit (a batch too: its pool kernels take
+    the same branches)."""
+    from twoscalesplit_gb300.solver import Batch
+    sc = scenes.dam_break_small(24, 48, seed=9)
+    sc.config.roi[:] = [0.3, -np.inf, np.inf, np.inf]
+    seq, par = Solver.from_scene(sc), Solver.from_scene(sc)
+    for sol in (seq, par):
+        sol.set_arith(arith)
+    seq.profile(True)
+    seq.step(40)
+    par.step(40)
+    seq.sync()
+    par.sync()
+    assert par.counts()["n_high"] > 0
+    for scale in (_abi.TSS_SCALE_LOW, _abi.TSS_SCALE_HIGH):
+        a, b = seq.download(scale), par.download(scale)
+        for k in ("id", "pos", "vel", "state", "dens", "pres"):
+            assert np.array_equal(a[k], b[k]), (scale, k)
+    scs = [scenes.dam_break_small(12 + 4 * k, 24, seed=k) for k in range(3)]
+    bs, bp = Batch(scs), Batch(scs)
+    for bb in (bs, bp):
+        bb.set_arith(arith)
+    bs.profile(True)
+    bs.step(30)
+    bp.step(30)
+    for k in range(len(scs)):
+        for scale in (_abi.TSS_SCALE_LOW, _abi.TSS_SCALE_HIGH):
+            x, y = bs.download_scene(k, scale), bp.download_scene(k, scale)
+            for name in ("id", "pos", "vel", "state"):
+                assert np.array_equal(x[name], y[name]), (k, scale, name)

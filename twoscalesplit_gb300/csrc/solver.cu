@@ -108,14 +108,34 @@ cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
     // when that pass runs one particle per thread
     if (launch.per_warp[1]) V.L.nbr = nullptr;
     if (launch.per_warp[0]) V.H.nbr = nullptr;
+    // Outside profiling, the two grid builds and the two density passes each run as
+    // two branches of the step graph: the low-res one on the side stream beside the
+    // high-res one, joined before the first kernel that reads both (and the split
+    // compaction beside the high-res force, below).  Neither of a pair reads what
+    // the other writes (they share only atomic ORs into the error word), so the
+    // results are those of the sequential order; the branches fill each other's
+    // partial last waves and the grid builds' launch gaps.  Profiling keeps the
+    // sequential order, so that each stage has its own interval.
+    const bool branch = !profile && side != nullptr;
+    auto fork = [&]() -> cudaError_t {
+        cudaError_t e2 = cudaEventRecord(fork_ev, s);
+        return e2 == cudaSuccess ? cudaStreamWaitEvent(side, fork_ev, 0) : e2;
+    };
+    auto join = [&]() -> cudaError_t {
+        cudaError_t e2 = cudaEventRecord(join_ev, side);
+        return e2 == cudaSuccess ? cudaStreamWaitEvent(s, join_ev, 0) : e2;
+    };
+    const cudaStream_t sl = branch ? side : s;  // the low-res branch's stream
     if ((e = mark(0, s)) != cudaSuccess) return e;
     // 1. neighbour grids: high then low (updateNeighborGridHigh / updateNeighborGrid);
     //    their key pass ran at the end of the previous step (force kernels, split),
     //    in prime_keys() after the state was set, or in a pool admission
+    if (branch && (e = fork()) != cudaSuccess) return e;
     e = grid_sort_enqueue(H.nid, &cnt->cur[1], capH, H.g, reorder_args(H, true), &cnt->err, s);
     if (e != cudaSuccess || (e = mark(1, s)) != cudaSuccess) return e;
-    e = grid_sort_enqueue(L.nid, &cnt->cur[0], nL, L.g, reorder_args(L, false), &cnt->err, s);
+    e = grid_sort_enqueue(L.nid, &cnt->cur[0], nL, L.g, reorder_args(L, false), &cnt->err, sl);
     if (e != cudaSuccess || (e = mark(2, s)) != cudaSuccess) return e;
+    if (branch && (e = join()) != cudaSuccess) return e;
     // 2. relaxation of last step's children (older snapshot's relaxTransient)
     for (int it = 0; it < P.relax_iters; ++it) {
         launch_k_relax_density(batched, blocksH, 256, s, P, V);
@@ -125,19 +145,26 @@ cudaError_t tss_solver::enqueue_step(cudaStream_t s) {
     if ((e = mark(3, s)) != cudaSuccess) return e;
     // 3. densities, 4. low force + advance + split marks, 5. children, 6. high force
     const bool fast = arith == TSS_ARITH_FAST;
-    auto gather = [&](int g) {
-        launch_gather(g, batched, launch.per_warp[g] != 0, fast, gather_grid[g], launch.threads[g], s, P, V);
+    auto gather = [&](int g, cudaStream_t gs) {
+        launch_gather(g, batched, launch.per_warp[g] != 0, fast, gather_grid[g], launch.threads[g], gs, P, V);
     };
-    gather(0);
+    if (branch && (e = fork()) != cudaSuccess) return e;
+    gather(0, s);
     if ((e = mark(4, s)) != cudaSuccess) return e;
-    gather(1);
+    gather(1, sl);
     if ((e = mark(5, s)) != cudaSuccess) return e;
+    if (branch && (e = join()) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(split_tile, 0, sizeof(unsigned) * split_ntiles, s)) != cudaSuccess) return e;
-    gather(2);
+    gather(2, s);
     if ((e = mark(6, s)) != cudaSuccess) return e;
-    launch_k_split(batched, std::min(split_ntiles, 8 * sm_count()), kSplitThreads, s, P, V);
+    // The split compaction appends children past the high-res list that the
+    // high-res force walks, and the two share only atomic adds into the next grid's
+    // cell counts: outside profiling they run as two branches too.
+    if (branch && (e = fork()) != cudaSuccess) return e;
+    launch_k_split(batched, std::min(split_ntiles, 8 * sm_count()), kSplitThreads, sl, P, V);
     if ((e = mark(7, s)) != cudaSuccess) return e;
-    gather(3);
+    gather(3, s);
+    if (branch && (e = join()) != cudaSuccess) return e;
     k_step_finish<<<1, 32, 0, s>>>(cnt);
     if ((e = mark(8, s)) != cudaSuccess) return e;
     return cudaGetLastError();
@@ -602,6 +629,7 @@ tss_status tss_solver_step(tss_solver* s, int n_steps, void* stream) {
         int b = 0;  // bucket: 1 << b steps
         if (!s->profile) b = n_steps >= 8 ? 3 : (n_steps >= 4 ? 2 : (n_steps >= 2 ? 1 : 0));
         if (!s->exec[b]) {
+            if ((e = s->ensure_side()) != cudaSuccess) return s->cuda_fail(e, "side stream");
             cudaStream_t cap = s->stream;
             if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
                 return s->cuda_fail(e, "begin capture");
@@ -1109,6 +1137,46 @@ tss_status tss_solver_autotune(tss_solver* s, int steps_per_trial, tss_launch* b
                 b.per_warp[g] = c.per_warp[g];
             }
     }
+    // The per-gather choice was timed stage by stage in the profiled (sequential)
+    // step graph; an unprofiled step runs the grid builds and the densities as
+    // parallel branches, where shapes overlap differently.  So the whole step is
+    // timed unprofiled with the per-gather choice, the default shape and one
+    // particle per warp throughout, and the fastest of the three is kept.
+    if (st == TSS_OK) st = tss_solver_profile(s, 0);
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (st == TSS_OK && (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess))
+        st = s->fail(TSS_CUDA_ERROR, "event create");
+    tss_launch whole[3] = {b, default_launch(), default_launch()};
+    for (int g = 0; g < TSS_NUM_GATHERS; ++g) whole[2].per_warp[g] = 1;
+    float whole_best = 3.0e38f;
+    tss_launch pick = b;
+    for (int wi = 0; wi < 3 && st == TSS_OK; ++wi) {
+        if ((st = s->apply_launch(whole[wi])) != TSS_OK) break;
+        if ((st = tss_solver_step(s, 1, s->stream)) != TSS_OK) break;  // captures the graph
+        ++taken;
+        if (cudaEventRecord(t0, s->stream) != cudaSuccess) {
+            st = s->fail(TSS_CUDA_ERROR, "event record");
+            break;
+        }
+        for (int k = 0; k < steps_per_trial && st == TSS_OK; ++k) {
+            st = tss_solver_step(s, 1, s->stream);
+            ++taken;
+        }
+        if (st != TSS_OK) break;
+        float ms = 0.0f;
+        if (cudaEventRecord(t1, s->stream) != cudaSuccess || cudaEventSynchronize(t1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) {
+            st = s->fail(TSS_CUDA_ERROR, "event timing");
+            break;
+        }
+        if (wi == 0 || ms < (1.0f - kMargin) * whole_best) {
+            whole_best = ms;
+            pick = whole[wi];
+        }
+    }
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    b = pick;
     if (st == TSS_OK) st = tss_solver_sync(s);  // a numeric or capacity error of the trial steps
     if (st != TSS_OK) {
         const std::string why = s->err;

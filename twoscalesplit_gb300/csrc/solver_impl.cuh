@@ -244,9 +244,24 @@ struct tss_solver {
         }
     }
 
+    // The second branch of a step graph (enqueue_step): a stream that joins the
+    // capture, and the events that fork it off and join it back.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaError_t ensure_side() {
+        cudaError_t e = cudaSuccess;
+        if (!side) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+        if (e == cudaSuccess && !fork_ev) e = cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming);
+        if (e == cudaSuccess && !join_ev) e = cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming);
+        return e;
+    }
+
     ~tss_solver() {
         wait_idle();
         drop_graph();
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
+        if (side) cudaStreamDestroy(side);
         if (work_ev) cudaEventDestroy(work_ev);
         for (auto& x : ev)
             if (x) cudaEventDestroy(x);

@@ -1,8 +1,10 @@
 """Launch shapes per GPU: the autotuner's choices kept on disk.
 
 tss_solver_autotune times the candidate launch shapes of the four gathers (64, 128
-or 256 threads per block; grids covering the list or one persistent wave) on a
-handle's own steps and installs the fastest per gather.  This module keeps the
+or 256 threads per block; grids covering the list or one persistent wave; one
+particle per warp) on a handle's own steps, picks the fastest per gather, and
+installs that choice unless the default shape or one particle per warp
+throughout runs whole steps faster.  This module keeps the
 chosen shape per (GPU model, workload class) in a JSON file, so that later handles
 of the same class start with it instead of tuning again.  The reference had one
 hard-coded shape (256-thread blocks, TwoScale2D/WCSPHSolver.cu:2421,2437).

@@ -646,9 +646,12 @@ __device__ __forceinline__ void force_high_one(const Params& P, const StepView& 
 // single-scene form at 48 registers (five blocks) spills 64 bytes instead of 120
 // at 40 and measured 3-4 % faster.  In the tolerance arithmetic the single-scene
 // form needs no spill at 40 registers (six blocks per SM) and is 3.8 % faster there
-// on the developed 1M dam break (0.159 -> 0.153 ms).
+// on the developed 1M dam break (0.159 -> 0.153 ms).  The batched form in the
+// tolerance arithmetic runs five blocks per SM (48 registers, 28 bytes spilled):
+// 4 % faster than four on the 512-scene batch (2.16 against 2.26 ms), where the
+// exact arithmetic's batched form was 8 % slower at five.
 template <bool B, class G, class A>
-__global__ void __launch_bounds__(256, B ? 4 : (A::kFast ? 6 : 5)) k_force_high(Params P0, StepView V) {
+__global__ void __launch_bounds__(256, B ? (A::kFast ? 5 : 4) : (A::kFast ? 6 : 5)) k_force_high(Params P0, StepView V) {
     for_each_particle<G>(V.cnt->cur[1], [&](int i) {
         if constexpr (B) {
             const Params& P = V.table[V.scH[i]];

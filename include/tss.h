@@ -399,11 +399,13 @@ tss_status tss_solver_read_positions(tss_solver* s, float* host_low, int cap_low
  * kernel copies the positions and lengths into one of two device staging buffers
  * of the solver (device-to-device, a few microseconds for a million particles);
  * a stream of the solver's own then writes them from there into the page-locked
- * host memory while `stream` goes on with the next steps.  *ticket names the
- * read-back for tss_solver_read_wait, which blocks the calling thread until its
- * host memory is written.  The staging buffers are used in turn: a read-back waits
- * on `stream` until the one two calls earlier has left its buffer.  The host
- * buffers must stay untouched until the ticket has been waited for. */
+ * host memory while `stream` goes on with the next steps (for a single scene by
+ * copy engine: the whole low-res list and host_high's first cap_high entries, of
+ * which those past counts[1] are undefined).  *ticket names the read-back for
+ * tss_solver_read_wait, which blocks the calling thread until its host memory is
+ * written.  The staging buffers are used in turn: a read-back waits on `stream`
+ * until the one two calls earlier has left its buffer.  The host buffers must stay
+ * untouched until the ticket has been waited for. */
 tss_status tss_solver_read_positions_async(tss_solver* s, float* host_low, int cap_low, float* host_high,
                                            int cap_high, int* counts, void* stream, int64_t* ticket);
 tss_status tss_solver_read_wait(tss_solver* s, int64_t ticket);
